@@ -1,0 +1,158 @@
+"""ctypes view of the C ABI declared in ``include/biospring_gb300.h``.
+
+The shared library is loaded from the package directory; there is no fallback: a
+missing or unloadable library raises, so nothing silently runs on the CPU.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libbiospring_gb300.so")
+
+BS_OK = 0
+BS_E_ARG = 1
+BS_E_CUDA = 2
+BS_E_NONFINITE = 3
+BS_E_CAPACITY = 4
+BS_E_TIMEOUT = 5
+BS_E_STATE = 6
+
+BS_STERIC_LINEAR = 0
+BS_STERIC_LJ_12_6_AMBER = 1
+BS_STERIC_LJ_8_6_LEWITT = 2
+BS_STERIC_LJ_8_6_ZACHARIAS = 3
+STERIC_MODES = {
+    "linear": BS_STERIC_LINEAR,
+    "lennard-jones-12-6Amber": BS_STERIC_LJ_12_6_AMBER,
+    "lennard-jones-8-6Lewitt": BS_STERIC_LJ_8_6_LEWITT,
+    "lennard-jones-8-6Zacharias": BS_STERIC_LJ_8_6_ZACHARIAS,
+}
+
+BS_DIELECTRIC_CONSTANT = 0
+BS_DIELECTRIC_DISTANCE = 1
+
+BS_TERM_STERIC = 0
+BS_TERM_COULOMB = 1
+BS_TERM_HYDROPHOBIC = 2
+
+ENERGY_NAMES = ("kinetic", "spring", "steric", "electrostatic", "imp", "hydrophobic")
+
+
+class BsConfig(C.Structure):
+    """Mirror of ``bs_config`` (field order and types must match the header)."""
+
+    _fields_ = [
+        ("nbsteps", C.c_int32),
+        ("timestep", C.c_double),
+        ("neighborskin", C.c_double),
+        ("spring_enable", C.c_int32),
+        ("spring_scale", C.c_double),
+        ("steric_enable", C.c_int32),
+        ("steric_gridscale", C.c_double),
+        ("steric_cutoff", C.c_double),
+        ("steric_mode", C.c_int32),
+        ("coulomb_enable", C.c_int32),
+        ("coulomb_scale", C.c_double),
+        ("coulomb_cutoff", C.c_double),
+        ("coulomb_dielectric", C.c_double),
+        ("hydrophobicity_enable", C.c_int32),
+        ("hydrophobicity_scale", C.c_double),
+        ("hydrophobicity_cutoff", C.c_double),
+        ("impala_enable", C.c_int32),
+        ("impala_scale", C.c_double),
+        ("viscosity_enable", C.c_int32),
+        ("viscosity_value", C.c_double),
+        ("rigidbody_enable", C.c_int32),
+        ("dielectric_mode", C.c_int32),
+        ("impala_z0", C.c_double),
+        ("impala_alpha", C.c_double),
+        ("rebuild_every", C.c_int32),
+        ("list_skin", C.c_double),
+    ]
+
+    def to_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_f32p = C.POINTER(C.c_float)
+_i32p = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+_u8p = C.POINTER(C.c_uint8)
+_f64p = C.POINTER(C.c_double)
+
+# name -> (restype, argtypes); every function of the header
+SIGNATURES = {
+    "bs_default_config": (C.c_int, [C.POINTER(BsConfig)]),
+    "bs_config_parse_msp": (C.c_int, [C.c_char_p, C.POINTER(BsConfig), C.c_char_p, C.c_size_t]),
+    "bs_create": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "bs_destroy": (C.c_int, [C.c_void_p]),
+    "bs_upload_particles": (C.c_int, [C.c_void_p, C.c_int64, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
+                                      _f32p, _f32p, _u8p]),
+    "bs_upload_springs": (C.c_int, [C.c_void_p, C.c_int64, _i32p, _f32p, _f32p]),
+    "bs_set_rigid_bodies": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _i32p]),
+    "bs_setup": (C.c_int, [C.c_void_p, C.POINTER(BsConfig)]),
+    "bs_step": (C.c_int, [C.c_void_p, C.c_int32]),
+    "bs_compute_forces": (C.c_int, [C.c_void_p]),
+    "bs_get_positions": (C.c_int, [C.c_void_p, _f32p]),
+    "bs_get_velocities": (C.c_int, [C.c_void_p, _f32p]),
+    "bs_get_forces": (C.c_int, [C.c_void_p, _f32p]),
+    "bs_set_positions": (C.c_int, [C.c_void_p, _f32p]),
+    "bs_set_velocities": (C.c_int, [C.c_void_p, _f32p]),
+    "bs_set_force": (C.c_int, [C.c_void_p, C.c_int64, _f32p]),
+    "bs_get_energies": (C.c_int, [C.c_void_p, _f64p]),
+    "bs_get_pairs": (C.c_int, [C.c_void_p, C.c_int32, _i64p, C.c_int64, _i64p]),
+    "bs_get_cells": (C.c_int, [C.c_void_p, C.c_int32, _i64p]),
+    "bs_get_launch_count": (C.c_int, [C.c_void_p, _i64p]),
+    "bs_last_error": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Loads the CUDA library (raises if it is missing: there is no CPU fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build it first (python -c 'import __graft_entry__ as g; g.build()')")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class BsError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+def ptr(a: np.ndarray | None, ctype):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def default_config() -> BsConfig:
+    cfg = BsConfig()
+    load().bs_default_config(C.byref(cfg))
+    return cfg
+
+
+def parse_msp(text: str, base: BsConfig | None = None) -> BsConfig:
+    cfg = base if base is not None else default_config()
+    err = C.create_string_buffer(512)
+    rc = load().bs_config_parse_msp(text.encode(), C.byref(cfg), err, 512)
+    if rc != BS_OK:
+        raise BsError(rc, err.value.decode())
+    return cfg

@@ -1,0 +1,943 @@
+// bs_capi.cu -- host side of the C ABI (include/biospring_gb300.h): handle, device buffers,
+// CUDA-graph step schedule, error reporting. No torch types, no allocation on the step path.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_set>
+#include <vector>
+
+#include "../../include/biospring_gb300.h"
+#include "bs_kernels.cuh"
+
+using namespace bsg;
+
+namespace
+{
+
+thread_local std::string g_last_error;
+
+struct DeviceBuffers
+{
+    std::vector<void *> owned;
+    template <typename T> cudaError_t alloc(T **ptr, size_t count)
+    {
+        void *p = nullptr;
+        const cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess)
+        {
+            owned.push_back(p);
+            *ptr = static_cast<T *>(p);
+        }
+        return e;
+    }
+    void free_all()
+    {
+        for (void *p : owned)
+            cudaFree(p);
+        owned.clear();
+    }
+};
+
+} // namespace
+
+struct bs_sim
+{
+    std::string err;
+    cudaStream_t stream = nullptr;
+    // host copies (caller order)
+    int64_t n = 0;
+    std::vector<float> xyz, vel, mass, charge, radius, eps, hydro, sasa, transfer;
+    std::vector<uint8_t> is_static, rigid;
+    std::vector<int32_t> sp_i, sp_j;
+    std::vector<float> sp_r0, sp_k;
+    std::unordered_set<uint64_t> sp_seen;
+    std::vector<std::vector<int32_t>> bodies;
+    bs_config cfg{};
+    bool have_cfg = false;
+    bool ready = false;
+    // device side
+    DeviceBuffers dev;
+    Params p{};
+    Ctl *ctl_host = nullptr; // pinned mirror
+    float *staging = nullptr; // device float[3n]
+    float4 *ext_host = nullptr; // pinned
+    bool ext_dirty = false;
+    int step_blocks = 0;
+    // schedule
+    bool list_valid = false;
+    int since_rebuild = 0;
+    long long steps_done = 0;
+    cudaGraphExec_t period_graph = nullptr;
+    int period_kernels = 0;
+    long long launches = 0;
+    // diagnostics scratch
+    long long *diag_out = nullptr;
+    unsigned long long *diag_count = nullptr;
+    size_t diag_cap = 0;
+};
+
+namespace
+{
+
+int fail(bs_sim *s, int code, const std::string &msg)
+{
+    if (s)
+        s->err = msg;
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(bs_sim *s, cudaError_t e, const char *what)
+{
+    return fail(s, BS_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define BS_CUDA(call)                                                                                                  \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        const cudaError_t e_ = (call);                                                                                 \
+        if (e_ != cudaSuccess)                                                                                         \
+            return cuda_fail(s, e_, #call);                                                                            \
+    } while (0)
+
+void destroy_graph(bs_sim *s)
+{
+    if (s->period_graph)
+    {
+        cudaGraphExecDestroy(s->period_graph);
+        s->period_graph = nullptr;
+    }
+}
+
+void release_device(bs_sim *s)
+{
+    destroy_graph(s);
+    s->dev.free_all();
+    if (s->ctl_host)
+    {
+        cudaFreeHost(s->ctl_host);
+        s->ctl_host = nullptr;
+    }
+    if (s->ext_host)
+    {
+        cudaFreeHost(s->ext_host);
+        s->ext_host = nullptr;
+    }
+    s->ready = false;
+}
+
+float band_lo2(double c) { return static_cast<float>((c * (1.0 - 1.0 / 16384.0)) * (c * (1.0 - 1.0 / 16384.0))); }
+float band_hi2(double c) { return static_cast<float>((c * (1.0 + 1.0 / 16384.0)) * (c * (1.0 + 1.0 / 16384.0))); }
+
+// Reads the control block back (synchronises the handle's stream).
+int read_ctl(bs_sim *s)
+{
+    BS_CUDA(cudaMemcpyAsync(s->ctl_host, s->p.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s->stream));
+    BS_CUDA(cudaStreamSynchronize(s->stream));
+    return BS_OK;
+}
+
+int clear_status(bs_sim *s, int bits)
+{
+    s->ctl_host->status &= ~bits;
+    BS_CUDA(cudaMemcpyAsync(&s->p.ctl->status, &s->ctl_host->status, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    return BS_OK;
+}
+
+// (Re)allocates the pair list and the cell arrays for the given capacities.
+int alloc_lists(bs_sim *s, int pl_cap, int cell_cap)
+{
+    Params &p = s->p;
+    // Pair list and grid arrays are the only buffers that grow; they are allocated apart.
+    static_assert(sizeof(int) == 4, "int32 expected");
+    int *pl = nullptr, *cs = nullptr, *cc = nullptr, *cf = nullptr;
+    BS_CUDA(s->dev.alloc(&pl, static_cast<size_t>(p.npad) * pl_cap));
+    BS_CUDA(s->dev.alloc(&cc, static_cast<size_t>(cell_cap) + 1));
+    BS_CUDA(s->dev.alloc(&cs, static_cast<size_t>(cell_cap) + 1));
+    BS_CUDA(s->dev.alloc(&cf, static_cast<size_t>(cell_cap) + 1));
+    BS_CUDA(cudaMemsetAsync(cc, 0, (static_cast<size_t>(cell_cap) + 1) * sizeof(int), s->stream));
+    // Old arrays are kept alive by the handle until destroy (growth is rare).
+    p.pl = pl;
+    p.pl_cap = pl_cap;
+    p.cell_cnt = cc;
+    p.cell_start = cs;
+    p.cell_fill = cf;
+    p.cell_cap = cell_cap;
+    destroy_graph(s);
+    return BS_OK;
+}
+
+int sync_ext(bs_sim *s)
+{
+    if (!s->ext_dirty)
+        return BS_OK;
+    BS_CUDA(cudaMemcpyAsync(s->p.ext, s->ext_host, sizeof(float4) * s->n, cudaMemcpyHostToDevice, s->stream));
+    int one = 1;
+    s->ctl_host->ext_pending = 1;
+    BS_CUDA(cudaMemcpyAsync(&s->p.ctl->ext_pending, &s->ctl_host->ext_pending, sizeof(int), cudaMemcpyHostToDevice,
+                            s->stream));
+    (void)one;
+    BS_CUDA(cudaStreamSynchronize(s->stream));
+    std::memset(s->ext_host, 0, sizeof(float4) * s->n);
+    s->ext_dirty = false;
+    return BS_OK;
+}
+
+// Runs a rebuild now and repairs capacity overflows until the list is valid.
+int rebuild_now(bs_sim *s)
+{
+    for (int attempt = 0; attempt < 8; ++attempt)
+    {
+        s->launches += launch_rebuild(s->p, s->stream);
+        BS_CUDA(cudaGetLastError());
+        int rc = read_ctl(s);
+        if (rc)
+            return rc;
+        const int st = s->ctl_host->status;
+        if (st & ST_NONFINITE)
+            return fail(s, BS_E_NONFINITE, "non-finite particle position");
+        if (st & ST_CELL_CAPACITY)
+        {
+            const long long need = s->ctl_host->ncells_needed;
+            if (need > (1ll << 28))
+                return fail(s, BS_E_CAPACITY, "search grid needs more than 2^28 cells (particles spread too far)");
+            rc = alloc_lists(s, s->p.pl_cap, static_cast<int>(need + need / 2 + 64));
+            if (rc)
+                return rc;
+            rc = clear_status(s, ST_CELL_CAPACITY);
+            if (rc)
+                return rc;
+            continue;
+        }
+        if (st & ST_PAIR_CAPACITY)
+        {
+            const int need = s->ctl_host->max_row;
+            if (static_cast<double>(need) * s->p.npad > 2.0e9)
+                return fail(s, BS_E_CAPACITY, "pair list would exceed 2^31 entries");
+            rc = alloc_lists(s, need + need / 4 + 16, s->p.cell_cap);
+            if (rc)
+                return rc;
+            rc = clear_status(s, ST_PAIR_CAPACITY);
+            if (rc)
+                return rc;
+            continue;
+        }
+        s->list_valid = true;
+        s->since_rebuild = 0;
+        return BS_OK;
+    }
+    return fail(s, BS_E_CAPACITY, "pair list or grid did not fit after repeated growth");
+}
+
+int capture_period_graph(bs_sim *s)
+{
+    destroy_graph(s);
+    const int K = std::max(1, s->cfg.rebuild_every);
+    cudaGraph_t g = nullptr;
+    BS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int kernels = launch_rebuild(s->p, s->stream);
+    for (int k = 0; k < K; ++k)
+        kernels += launch_step(s->p, MODE_STEP, s->stream);
+    BS_CUDA(cudaStreamEndCapture(s->stream, &g));
+    const cudaError_t e = cudaGraphInstantiate(&s->period_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+        return cuda_fail(s, e, "cudaGraphInstantiate");
+    s->period_kernels = kernels;
+    return BS_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int bs_default_config(bs_config *c)
+{
+    if (!c)
+        return fail(nullptr, BS_E_ARG, "bs_default_config: null config");
+    std::memset(c, 0, sizeof(*c));
+    // configuration::defaultConfiguration() (Configuration.hpp:153-234)
+    c->nbsteps = -1;
+    c->timestep = 0.01;
+    c->neighborskin = 0.0;
+    c->steric_enable = 0;
+    c->steric_gridscale = 1.0;
+    c->steric_cutoff = 1.0;
+    c->steric_mode = BS_STERIC_LINEAR;
+    c->spring_enable = 0;
+    c->spring_scale = 1.0;
+    c->hydrophobicity_enable = 0;
+    c->hydrophobicity_cutoff = 15.0;
+    c->hydrophobicity_scale = 1.0;
+    c->coulomb_enable = 0;
+    c->coulomb_cutoff = 16.0;
+    c->coulomb_scale = 1.0;
+    c->coulomb_dielectric = 1.0;
+    c->viscosity_enable = 0;
+    c->viscosity_value = 1.0;
+    c->rigidbody_enable = 0;
+    c->impala_enable = 0;
+    c->impala_scale = 1.0;
+    // device-path knobs
+    c->dielectric_mode = BS_DIELECTRIC_CONSTANT;
+    c->impala_z0 = 15.75;
+    c->impala_alpha = 1.99;
+    c->rebuild_every = 10;
+    c->list_skin = 1.0;
+    return BS_OK;
+}
+
+int bs_create(bs_sim **out)
+{
+    if (!out)
+        return fail(nullptr, BS_E_ARG, "bs_create: null output");
+    auto *s = new bs_sim();
+    const cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess)
+    {
+        const int rc = cuda_fail(nullptr, e, "cudaStreamCreate");
+        delete s;
+        return rc;
+    }
+    bs_default_config(&s->cfg);
+    *out = s;
+    return BS_OK;
+}
+
+int bs_destroy(bs_sim *s)
+{
+    if (!s)
+        return BS_OK;
+    if (s->stream)
+        cudaStreamSynchronize(s->stream);
+    release_device(s);
+    if (s->stream)
+        cudaStreamDestroy(s->stream);
+    delete s;
+    return BS_OK;
+}
+
+int bs_upload_particles(bs_sim *s, int64_t n, const float *xyz, const float *vel, const float *mass,
+                        const float *charge, const float *radius, const float *epsilon, const float *hydrophobicity,
+                        const float *sasa, const float *transfer, const uint8_t *is_static)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->sp_i.empty())
+        return fail(s, BS_E_STATE, "SpringNetwork::addParticle: particles must be added before springs");
+    if (n < 0 || n > (1ll << 29) || (n > 0 && !xyz))
+        return fail(s, BS_E_ARG, "bs_upload_particles: bad particle count or null coordinates");
+    auto put = [&](std::vector<float> &v, const float *src, int64_t per, float def) {
+        const size_t off = v.size();
+        v.resize(off + static_cast<size_t>(n * per), def);
+        if (src)
+            std::memcpy(v.data() + off, src, sizeof(float) * n * per);
+    };
+    put(s->xyz, xyz, 3, 0.0f);
+    put(s->vel, vel, 3, 0.0f);
+    put(s->mass, mass, 1, 1.0f);
+    put(s->charge, charge, 1, 0.0f);
+    put(s->radius, radius, 1, 1.0f);
+    put(s->eps, epsilon, 1, 0.0f);
+    put(s->hydro, hydrophobicity, 1, 0.0f);
+    put(s->sasa, sasa, 1, 0.0f);
+    put(s->transfer, transfer, 1, 0.0f);
+    const size_t off = s->is_static.size();
+    s->is_static.resize(off + n, 0);
+    if (is_static)
+        for (int64_t i = 0; i < n; ++i)
+            s->is_static[off + i] = is_static[i] ? 1 : 0;
+    s->n += n;
+    s->rigid.assign(s->n, 0);
+    s->ready = false;
+    return BS_OK;
+}
+
+int bs_upload_springs(bs_sim *s, int64_t ns, const int32_t *ij, const float *equilibrium, const float *stiffness)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (ns < 0 || (ns > 0 && (!ij || !equilibrium || !stiffness)))
+        return fail(s, BS_E_ARG, "bs_upload_springs: bad arguments");
+    for (int64_t t = 0; t < ns; ++t)
+    {
+        const int64_t a = ij[2 * t], b = ij[2 * t + 1];
+        if (a < 0 || b < 0 || a >= s->n || b >= s->n)
+            return fail(s, BS_E_ARG, "SpringNetwork::addSpring: particle index out of range");
+        if (a == b)
+            return fail(s, BS_E_ARG, "SpringNetwork::addSpring: a spring requires two distinct particles");
+    }
+    for (int64_t t = 0; t < ns; ++t)
+    {
+        const uint32_t a = static_cast<uint32_t>(ij[2 * t]), b = static_cast<uint32_t>(ij[2 * t + 1]);
+        const uint64_t key = (static_cast<uint64_t>(std::min(a, b)) << 32) | std::max(a, b);
+        if (!s->sp_seen.insert(key).second)
+            continue; // already bonded: SpringNetwork::addSpring ignores it
+        s->sp_i.push_back(static_cast<int32_t>(a));
+        s->sp_j.push_back(static_cast<int32_t>(b));
+        s->sp_r0.push_back(equilibrium[t]);
+        s->sp_k.push_back(stiffness[t]);
+    }
+    s->ready = false;
+    return BS_OK;
+}
+
+int bs_set_rigid_bodies(bs_sim *s, int32_t nb, const int32_t *offsets, const int32_t *ids)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (nb < 0 || (nb > 0 && (!offsets || !ids)))
+        return fail(s, BS_E_ARG, "bs_set_rigid_bodies: bad arguments");
+    std::vector<std::vector<int32_t>> bodies(nb);
+    std::vector<uint8_t> seen(s->n, 0);
+    for (int32_t b = 0; b < nb; ++b)
+    {
+        if (offsets[b + 1] < offsets[b])
+            return fail(s, BS_E_ARG, "bs_set_rigid_bodies: offsets must be non-decreasing");
+        for (int32_t t = offsets[b]; t < offsets[b + 1]; ++t)
+        {
+            const int32_t id = ids[t];
+            if (id < 0 || id >= s->n)
+                return fail(s, BS_E_ARG, "bs_set_rigid_bodies: particle id out of range");
+            if (seen[id])
+                return fail(s, BS_E_ARG, "bs_set_rigid_bodies: a particle belongs to two bodies");
+            seen[id] = 1;
+            bodies[b].push_back(id);
+        }
+    }
+    s->bodies = bodies;
+    s->ready = false;
+    return fail(s, BS_E_STATE, "bs_set_rigid_bodies: rigid-body dynamics are not available in this build");
+}
+
+int bs_setup(bs_sim *s, const bs_config *cfg)
+{
+    if (!s || !cfg)
+        return fail(s, BS_E_ARG, "bs_setup: null argument");
+    const bs_config &c = *cfg;
+    // Validation as in SpringNetwork::_setupSteric/_setupElectrostatic/_setupHydrophobic
+    // (SpringNetwork.cpp:663-737) and NeighborSearchBase (nsearch.hpp:61-68).
+    if (c.steric_enable && c.steric_cutoff < 1e-6)
+        return fail(s, BS_E_ARG, "Steric cutoff must be > 0");
+    if (c.coulomb_enable && c.coulomb_cutoff < 1e-6)
+        return fail(s, BS_E_ARG, "Electrostatic cutoff must be > 0");
+    if (c.hydrophobicity_enable && c.hydrophobicity_cutoff < 1e-6)
+        return fail(s, BS_E_ARG, "Hydrophobic cutoff must be > 0");
+    if (c.steric_enable && s->n == 0)
+        return fail(s, BS_E_ARG, "the particle list is empty");
+    if (c.steric_mode < BS_STERIC_LINEAR || c.steric_mode > BS_STERIC_LJ_8_6_ZACHARIAS)
+        return fail(s, BS_E_ARG, "steric.mode: invalid choice");
+    if (c.dielectric_mode != BS_DIELECTRIC_CONSTANT && c.dielectric_mode != BS_DIELECTRIC_DISTANCE)
+        return fail(s, BS_E_ARG, "cuda.dielectricmode: invalid choice");
+    if (c.rebuild_every < 1)
+        return fail(s, BS_E_ARG, "cuda.rebuildevery must be >= 1");
+    if (!(c.list_skin >= 0.0))
+        return fail(s, BS_E_ARG, "cuda.listskin must be >= 0");
+    if (c.rigidbody_enable && !s->bodies.empty())
+        return fail(s, BS_E_STATE, "rigid-body dynamics are not available in this build");
+    if (s->n == 0)
+        return fail(s, BS_E_ARG, "bs_setup: no particles");
+
+    release_device(s);
+    s->cfg = c;
+    s->have_cfg = true;
+    const int64_t n = s->n;
+    Params &p = s->p;
+    p = Params{};
+    p.n = static_cast<int>(n);
+    p.npad = static_cast<int>((n + 31) / 32 * 32);
+    const int npad = p.npad;
+
+    // ---- spring CSR in caller order (both directions) ----
+    std::vector<int> deg(n, 0);
+    for (size_t t = 0; t < s->sp_i.size(); ++t)
+    {
+        deg[s->sp_i[t]]++;
+        deg[s->sp_j[t]]++;
+    }
+    std::vector<int> row(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i)
+        row[i + 1] = row[i] + deg[i];
+    const int nnz = row[n];
+    std::vector<int> col(std::max(nnz, 1));
+    std::vector<float> kk(std::max(nnz, 1)), rr(std::max(nnz, 1));
+    std::vector<int> fillp(row.begin(), row.end() - 1);
+    auto partner_code = [&](int a, int b) {
+        uint32_t code = static_cast<uint32_t>(b);
+        if (s->is_static[b])
+            code |= 0x80000000u;
+        if (s->rigid[a] && s->rigid[b])
+            code |= 0x40000000u;
+        return static_cast<int>(code);
+    };
+    for (size_t t = 0; t < s->sp_i.size(); ++t)
+    {
+        const int a = s->sp_i[t], b = s->sp_j[t];
+        int e = fillp[a]++;
+        col[e] = partner_code(a, b);
+        kk[e] = s->sp_k[t];
+        rr[e] = s->sp_r0[t];
+        e = fillp[b]++;
+        col[e] = partner_code(b, a);
+        kk[e] = s->sp_k[t];
+        rr[e] = s->sp_r0[t];
+    }
+    int maxdeg = 1;
+    for (int64_t i = 0; i < n; ++i)
+        maxdeg = std::max(maxdeg, deg[i]);
+    p.sp_maxdeg = maxdeg;
+
+    // ---- per-particle packed parameters ----
+    std::vector<float4> pos0(npad), vel0(npad), jprm0(npad), iprm0(npad);
+    for (int64_t i = 0; i < n; ++i)
+    {
+        pos0[i] = make_float4(s->xyz[3 * i], s->xyz[3 * i + 1], s->xyz[3 * i + 2], s->charge[i]);
+        vel0[i] = make_float4(s->vel[3 * i], s->vel[3 * i + 1], s->vel[3 * i + 2], 0.f);
+        float a = 0.f, b = s->radius[i];
+        if (c.steric_mode == BS_STERIC_LJ_12_6_AMBER || c.steric_mode == BS_STERIC_LJ_8_6_LEWITT)
+        {
+            a = std::sqrt(s->eps[i]);
+            b = std::sqrt(s->radius[i]);
+        }
+        else if (c.steric_mode == BS_STERIC_LJ_8_6_ZACHARIAS)
+            a = s->eps[i];
+        uint32_t flags = 0;
+        if (s->is_static[i])
+            flags |= PF_STATIC;
+        if (s->charge[i] != 0.0f)
+            flags |= PF_CHARGED;
+        if (s->hydro[i] != 0.0f)
+            flags |= PF_HYDROPHOBIC;
+        if (s->rigid[i])
+            flags |= PF_RIGID;
+        float fw;
+        std::memcpy(&fw, &flags, sizeof(fw));
+        jprm0[i] = make_float4(a, b, s->hydro[i], fw);
+        iprm0[i] = make_float4(s->mass[i], s->sasa[i], s->transfer[i], 0.f);
+    }
+    std::vector<int> perm0(npad, 0), inv0(n);
+    for (int64_t i = 0; i < n; ++i)
+    {
+        perm0[i] = static_cast<int>(i);
+        inv0[i] = static_cast<int>(i);
+    }
+
+    // ---- device allocation ----
+    for (int b = 0; b < 2; ++b)
+    {
+        BS_CUDA(s->dev.alloc(&p.pos[b], npad));
+        BS_CUDA(s->dev.alloc(&p.vel[b], npad));
+        BS_CUDA(s->dev.alloc(&p.jprm[b], npad));
+        BS_CUDA(s->dev.alloc(&p.iprm[b], npad));
+        BS_CUDA(s->dev.alloc(&p.perm[b], npad));
+    }
+    BS_CUDA(s->dev.alloc(&p.inv, n));
+    BS_CUDA(s->dev.alloc(&p.pos_build, npad));
+    BS_CUDA(s->dev.alloc(&p.ext, n));
+    BS_CUDA(s->dev.alloc(&p.force_out, n));
+    int *d_row, *d_col;
+    float *d_k, *d_r0;
+    BS_CUDA(s->dev.alloc(&d_row, n + 1));
+    BS_CUDA(s->dev.alloc(&d_col, std::max(nnz, 1)));
+    BS_CUDA(s->dev.alloc(&d_k, std::max(nnz, 1)));
+    BS_CUDA(s->dev.alloc(&d_r0, std::max(nnz, 1)));
+    p.sp_row = d_row;
+    p.sp_col = d_col;
+    p.sp_k = d_k;
+    p.sp_r0 = d_r0;
+    BS_CUDA(s->dev.alloc(&p.se_col, static_cast<size_t>(npad) * maxdeg));
+    BS_CUDA(s->dev.alloc(&p.se_k, static_cast<size_t>(npad) * maxdeg));
+    BS_CUDA(s->dev.alloc(&p.se_r0, static_cast<size_t>(npad) * maxdeg));
+    BS_CUDA(s->dev.alloc(&p.se_deg, npad));
+    BS_CUDA(s->dev.alloc(&p.pl_cnt, npad));
+    BS_CUDA(s->dev.alloc(&p.cell_of, npad));
+    BS_CUDA(s->dev.alloc(&p.tmp_perm, npad));
+    s->step_blocks = (p.n + kStepBlock - 1) / kStepBlock;
+    BS_CUDA(s->dev.alloc(&p.blk_energy, static_cast<size_t>(s->step_blocks) * 8));
+    BS_CUDA(s->dev.alloc(&p.ctl, 1));
+    BS_CUDA(s->dev.alloc(&s->staging, 3 * static_cast<size_t>(n)));
+    BS_CUDA(cudaMallocHost(reinterpret_cast<void **>(&s->ctl_host), sizeof(Ctl)));
+    BS_CUDA(cudaMallocHost(reinterpret_cast<void **>(&s->ext_host), sizeof(float4) * n));
+    std::memset(s->ext_host, 0, sizeof(float4) * n);
+
+    // initial grid capacity from the current bounding box
+    const double list_radius = static_cast<float>(std::max({c.steric_enable ? c.steric_cutoff : 0.0,
+                                                            c.coulomb_enable ? c.coulomb_cutoff : 0.0,
+                                                            c.hydrophobicity_enable ? c.hydrophobicity_cutoff : 0.0,
+                                                            1e-3}) +
+                                                   c.list_skin);
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k)
+        {
+            lo[k] = std::min(lo[k], static_cast<double>(s->xyz[3 * i + k]));
+            hi[k] = std::max(hi[k], static_cast<double>(s->xyz[3 * i + k]));
+        }
+    double cells = 1.0;
+    for (int k = 0; k < 3; ++k)
+        cells *= std::ceil((hi[k] - lo[k]) / list_radius) + 3.0;
+    const int cell_cap = static_cast<int>(std::min(2.0 * cells + 1024.0, 2.0e8));
+    const int pl_cap = 64;
+    int rc = alloc_lists(s, pl_cap, cell_cap);
+    if (rc)
+        return rc;
+
+    // ---- uploads ----
+    BS_CUDA(cudaMemcpyAsync(p.pos[0], pos0.data(), sizeof(float4) * npad, cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(p.vel[0], vel0.data(), sizeof(float4) * npad, cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(p.jprm[0], jprm0.data(), sizeof(float4) * npad, cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(p.iprm[0], iprm0.data(), sizeof(float4) * npad, cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(p.perm[0], perm0.data(), sizeof(int) * npad, cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(p.inv, inv0.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(d_row, row.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(d_col, col.data(), sizeof(int) * std::max(nnz, 1), cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(d_k, kk.data(), sizeof(float) * std::max(nnz, 1), cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(d_r0, rr.data(), sizeof(float) * std::max(nnz, 1), cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemsetAsync(p.ext, 0, sizeof(float4) * n, s->stream));
+    BS_CUDA(cudaMemsetAsync(p.force_out, 0, sizeof(float4) * n, s->stream));
+    std::memset(s->ctl_host, 0, sizeof(Ctl));
+    for (int k = 0; k < 3; ++k)
+    {
+        s->ctl_host->bbox_enc[k] = 0xffffffffu;
+        s->ctl_host->bbox_enc[3 + k] = 0u;
+    }
+    BS_CUDA(cudaMemcpyAsync(p.ctl, s->ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, s->stream));
+
+    // ---- step parameters ----
+    p.dt = static_cast<float>(c.timestep);
+    p.spring_on = c.spring_enable != 0;
+    p.steric_on = c.steric_enable != 0;
+    p.coulomb_on = c.coulomb_enable != 0;
+    p.hydro_on = c.hydrophobicity_enable != 0;
+    p.imp_on = c.impala_enable != 0;
+    p.visc_on = c.viscosity_enable != 0;
+    p.steric_mode = c.steric_mode;
+    p.dielectric_mode = c.dielectric_mode;
+    p.c_steric = static_cast<float>(c.steric_cutoff);
+    p.c_coulomb = static_cast<float>(c.coulomb_cutoff);
+    p.c_hydro = static_cast<float>(c.hydrophobicity_cutoff);
+    p.lo2_s = band_lo2(p.c_steric);
+    p.hi2_s = band_hi2(p.c_steric);
+    p.lo2_c = band_lo2(p.c_coulomb);
+    p.hi2_c = band_hi2(p.c_coulomb);
+    p.lo2_h = band_lo2(p.c_hydro);
+    p.hi2_h = band_hi2(p.c_hydro);
+    float r2_any = 0.f;
+    if (p.steric_on)
+        r2_any = std::max(r2_any, p.hi2_s);
+    if (p.coulomb_on)
+        r2_any = std::max(r2_any, p.hi2_c);
+    if (p.hydro_on)
+        r2_any = std::max(r2_any, p.hi2_h);
+    p.r2_any = r2_any;
+    p.list_radius = static_cast<float>(list_radius);
+    p.list_r2 = static_cast<float>(list_radius * list_radius * (1.0 + 1e-5));
+    const double hs = 0.5 * c.list_skin * (1.0 - 1e-5);
+    p.half_skin2 = static_cast<float>(hs * hs);
+    p.spring_scale = static_cast<float>(c.spring_scale);
+    p.steric_scale = static_cast<float>(c.steric_gridscale);
+    p.coulomb_scale = static_cast<float>(c.coulomb_scale);
+    p.hydro_scale = static_cast<float>(c.hydrophobicity_scale);
+    p.imp_scale = static_cast<float>(c.impala_scale);
+    p.dielectric = static_cast<float>(c.coulomb_dielectric);
+    p.visc = static_cast<float>(c.viscosity_value);
+    p.imp_z0 = static_cast<float>(c.impala_z0);
+    p.imp_alpha = static_cast<float>(c.impala_alpha);
+    p.k_spring_f = static_cast<float>(kSpringForceConvert);
+    p.k_elec_e = static_cast<float>(kCoulombEnergyPerA);
+    p.k_elec_f = static_cast<float>(kElecForceConvert / (4.0 * kPi));
+    p.k_kin = static_cast<float>(kKineticConvert);
+    p.k_imp_f = static_cast<float>(kImpForceConvert);
+    p.k_hydro_e = static_cast<float>(kAvogadro * 1.0E-3);
+
+    s->ready = true;
+    s->steps_done = 0;
+    s->list_valid = false;
+    rc = rebuild_now(s);
+    if (rc)
+    {
+        s->ready = false;
+        return rc;
+    }
+    return BS_OK;
+}
+
+int bs_step(bs_sim *s, int32_t nsteps)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "bs_step: call bs_setup first");
+    if (nsteps < 0)
+        return fail(s, BS_E_ARG, "bs_step: negative step count");
+    int rc = sync_ext(s);
+    if (rc)
+        return rc;
+    const int K = std::max(1, s->cfg.rebuild_every);
+    const long long target = s->steps_done + nsteps;
+    for (int round = 0; round < 64 && s->steps_done < target; ++round)
+    {
+        long long remaining = target - s->steps_done;
+        long long queued = 0;
+        while (remaining > 0)
+        {
+            if (!s->list_valid || s->since_rebuild >= K)
+            {
+                if (remaining >= K)
+                {
+                    if (!s->period_graph)
+                    {
+                        rc = capture_period_graph(s);
+                        if (rc)
+                            return rc;
+                    }
+                    BS_CUDA(cudaGraphLaunch(s->period_graph, s->stream));
+                    s->launches += s->period_kernels;
+                    s->list_valid = true;
+                    s->since_rebuild = K;
+                    remaining -= K;
+                    queued += K;
+                    continue;
+                }
+                s->launches += launch_rebuild(s->p, s->stream);
+                s->list_valid = true;
+                s->since_rebuild = 0;
+            }
+            const long long chunk = std::min<long long>(remaining, K - s->since_rebuild);
+            for (long long k = 0; k < chunk; ++k)
+                s->launches += launch_step(s->p, MODE_STEP, s->stream);
+            s->since_rebuild += static_cast<int>(chunk);
+            remaining -= chunk;
+            queued += chunk;
+        }
+        BS_CUDA(cudaGetLastError());
+        rc = read_ctl(s);
+        if (rc)
+            return rc;
+        const Ctl &h = *s->ctl_host;
+        s->steps_done = h.steps;
+        if (h.status & ST_NONFINITE)
+            return fail(s, BS_E_NONFINITE, "Found non-finite position (a particle position became NaN or infinite)");
+        if (h.status & (ST_CELL_CAPACITY | ST_PAIR_CAPACITY))
+        {
+            rc = rebuild_now(s); // grows and rebuilds
+            if (rc)
+                return rc;
+            continue;
+        }
+        if (h.status & ST_STALE)
+            s->list_valid = false; // the next rebuild clears the bit
+    }
+    if (s->steps_done < target)
+        return fail(s, BS_E_STATE, "bs_step: could not complete the requested steps");
+    return BS_OK;
+}
+
+int bs_compute_forces(bs_sim *s)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "bs_compute_forces: call bs_setup first");
+    int rc = sync_ext(s);
+    if (rc)
+        return rc;
+    if (!s->list_valid || (s->ctl_host->status & ST_STALE))
+    {
+        rc = rebuild_now(s);
+        if (rc)
+            return rc;
+    }
+    s->launches += launch_step(s->p, MODE_FORCES, s->stream);
+    BS_CUDA(cudaGetLastError());
+    rc = read_ctl(s);
+    if (rc)
+        return rc;
+    if (s->ctl_host->status & ~ST_STALE)
+        return fail(s, BS_E_STATE, "bs_compute_forces: device status not clean");
+    return BS_OK;
+}
+
+static int get_vec(bs_sim *s, int what, float *out)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    if (!out)
+        return fail(s, BS_E_ARG, "null output");
+    s->launches += launch_unsort(s->p, what, s->staging, s->stream);
+    BS_CUDA(cudaGetLastError());
+    BS_CUDA(cudaMemcpyAsync(out, s->staging, sizeof(float) * 3 * s->n, cudaMemcpyDeviceToHost, s->stream));
+    BS_CUDA(cudaStreamSynchronize(s->stream));
+    return BS_OK;
+}
+
+int bs_get_positions(bs_sim *s, float *xyz) { return get_vec(s, 0, xyz); }
+int bs_get_velocities(bs_sim *s, float *v) { return get_vec(s, 1, v); }
+int bs_get_forces(bs_sim *s, float *f) { return get_vec(s, 2, f); }
+
+static int set_state(bs_sim *s, const float *xyz, const float *vel)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    const float *src = xyz ? xyz : vel;
+    if (!src)
+        return fail(s, BS_E_ARG, "null input");
+    BS_CUDA(cudaMemcpyAsync(s->staging, src, sizeof(float) * 3 * s->n, cudaMemcpyHostToDevice, s->stream));
+    s->launches += launch_set_positions(s->p, xyz ? s->staging : nullptr, xyz ? nullptr : s->staging, s->stream);
+    BS_CUDA(cudaGetLastError());
+    BS_CUDA(cudaStreamSynchronize(s->stream));
+    if (xyz)
+        s->list_valid = false;
+    return BS_OK;
+}
+
+int bs_set_positions(bs_sim *s, const float *xyz) { return set_state(s, xyz, nullptr); }
+int bs_set_velocities(bs_sim *s, const float *vel) { return set_state(s, nullptr, vel); }
+
+int bs_set_force(bs_sim *s, int64_t i, const float f[3])
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    if (i < 0 || i >= s->n || !f)
+        return fail(s, BS_E_ARG, "bs_set_force: particle index out of range");
+    s->ext_host[i].x += f[0];
+    s->ext_host[i].y += f[1];
+    s->ext_host[i].z += f[2];
+    s->ext_dirty = true;
+    return BS_OK;
+}
+
+int bs_get_energies(bs_sim *s, double out[BS_NUM_ENERGIES])
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    BS_CUDA(cudaMemcpyAsync(s->ctl_host->energies, s->p.ctl->energies, sizeof(double) * BS_NUM_ENERGIES,
+                            cudaMemcpyDeviceToHost, s->stream));
+    BS_CUDA(cudaStreamSynchronize(s->stream));
+    for (int k = 0; k < BS_NUM_ENERGIES; ++k)
+        out[k] = s->ctl_host->energies[k];
+    return BS_OK;
+}
+
+int bs_get_pairs(bs_sim *s, int32_t term, int64_t *out, int64_t cap, int64_t *n_out)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    if (term < BS_TERM_STERIC || term > BS_TERM_HYDROPHOBIC || cap < 0 || !n_out || (cap > 0 && !out))
+        return fail(s, BS_E_ARG, "bs_get_pairs: bad arguments");
+    if (!s->list_valid || (s->ctl_host->status & ST_STALE))
+    {
+        const int rc = rebuild_now(s);
+        if (rc)
+            return rc;
+    }
+    // Diagnostic scratch, sized on demand (diagnostics are not on the step path).
+    const size_t want = static_cast<size_t>(std::max<int64_t>(cap, 1));
+    if (s->diag_cap < want)
+    {
+        BS_CUDA(s->dev.alloc(&s->diag_out, 2 * want));
+        s->diag_cap = want;
+    }
+    if (!s->diag_count)
+        BS_CUDA(s->dev.alloc(&s->diag_count, 1));
+    BS_CUDA(cudaMemsetAsync(s->diag_count, 0, sizeof(unsigned long long), s->stream));
+    s->launches += launch_diag_pairs(s->p, term, s->diag_out, s->diag_count, static_cast<unsigned long long>(cap),
+                                     s->stream);
+    BS_CUDA(cudaGetLastError());
+    unsigned long long count = 0;
+    BS_CUDA(cudaMemcpyAsync(&count, s->diag_count, sizeof(count), cudaMemcpyDeviceToHost, s->stream));
+    BS_CUDA(cudaStreamSynchronize(s->stream));
+    const int64_t w = std::min<int64_t>(static_cast<int64_t>(count), cap);
+    if (w > 0)
+    {
+        BS_CUDA(cudaMemcpy(out, s->diag_out, sizeof(int64_t) * 2 * w, cudaMemcpyDeviceToHost));
+        // sort by (i, j): the device emits in slot order
+        std::vector<std::pair<int64_t, int64_t>> v(w);
+        for (int64_t t = 0; t < w; ++t)
+            v[t] = {out[2 * t], out[2 * t + 1]};
+        std::sort(v.begin(), v.end());
+        for (int64_t t = 0; t < w; ++t)
+        {
+            out[2 * t] = v[t].first;
+            out[2 * t + 1] = v[t].second;
+        }
+    }
+    *n_out = static_cast<int64_t>(count);
+    return BS_OK;
+}
+
+int bs_get_cells(bs_sim *s, int32_t term, int64_t *out)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    if (term < BS_TERM_STERIC || term > BS_TERM_HYDROPHOBIC || !out)
+        return fail(s, BS_E_ARG, "bs_get_cells: bad arguments");
+    const bs_config &c = s->cfg;
+    float cutoff = static_cast<float>(c.steric_cutoff);
+    uint32_t need = 0;
+    bool on = c.steric_enable != 0;
+    if (term == BS_TERM_COULOMB)
+    {
+        cutoff = static_cast<float>(c.coulomb_cutoff);
+        need = PF_CHARGED;
+        on = c.coulomb_enable != 0;
+    }
+    else if (term == BS_TERM_HYDROPHOBIC)
+    {
+        cutoff = static_cast<float>(c.hydrophobicity_cutoff);
+        need = PF_HYDROPHOBIC;
+        on = c.hydrophobicity_enable != 0;
+    }
+    if (!on)
+    {
+        for (int64_t i = 0; i < s->n; ++i)
+            out[i] = -1;
+        return BS_OK;
+    }
+    long long *d_out = nullptr;
+    if (s->diag_cap < static_cast<size_t>(s->n))
+    {
+        BS_CUDA(s->dev.alloc(&s->diag_out, 2 * static_cast<size_t>(s->n)));
+        s->diag_cap = static_cast<size_t>(s->n);
+    }
+    d_out = s->diag_out;
+    s->launches += launch_diag_cells(s->p, cutoff, static_cast<float>(c.neighborskin), need, d_out, s->stream);
+    BS_CUDA(cudaGetLastError());
+    BS_CUDA(cudaMemcpyAsync(out, d_out, sizeof(int64_t) * s->n, cudaMemcpyDeviceToHost, s->stream));
+    BS_CUDA(cudaStreamSynchronize(s->stream));
+    return BS_OK;
+}
+
+int bs_get_launch_count(bs_sim *s, int64_t *count)
+{
+    if (!s || !count)
+        return fail(s, BS_E_ARG, "bs_get_launch_count: null argument");
+    *count = s->launches;
+    return BS_OK;
+}
+
+int bs_last_error(bs_sim *s, char *buf, size_t len)
+{
+    if (!buf || len == 0)
+        return BS_E_ARG;
+    const std::string &m = s ? s->err : g_last_error;
+    std::snprintf(buf, len, "%s", m.c_str());
+    return BS_OK;
+}
+
+} // extern "C"

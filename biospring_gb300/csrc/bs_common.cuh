@@ -1,0 +1,138 @@
+// bs_common.cuh -- shared device definitions of the GB300 step engine.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/biospring_gb300.h"
+
+namespace bsg
+{
+
+// ---- unit constants (values of src/forcefield/constants.hpp:36-118) -------------------
+constexpr double kElectronChargeC = 1.60217653E-19;
+constexpr double kAngstromToMeter = 1.0E-10;
+constexpr double kMeterToAngstrom = 1.0E10;
+constexpr double kDaltonToKg = 1.66054E-27;
+constexpr double kFsToS = 1.0E-15;
+constexpr double kSToFs = 1.0E15;
+constexpr double kPi = 3.1415927;
+constexpr double kVacuumPermittivity = 8.854187817E-12;
+constexpr double kAvogadro = 6.02214169E23;
+constexpr double kCoulombK = 1.0 / (4.0 * kPi * kVacuumPermittivity);
+constexpr double kNewtonToDaAFs2 = kMeterToAngstrom * (1.0 / kDaltonToKg) * kFsToS * kFsToS;
+// force conversions: molar kJ/mol/A -> Da.A.fs^-2, and the Coulomb one
+constexpr double kSpringForceConvert = 1.0E3 / kAvogadro * kMeterToAngstrom * kNewtonToDaAFs2;
+constexpr double kImpForceConvert = kSpringForceConvert;
+constexpr double kElecForceConvert = kNewtonToDaAFs2 * (kElectronChargeC * kElectronChargeC) /
+                                     (kVacuumPermittivity * kAngstromToMeter * kAngstromToMeter);
+constexpr double kKineticConvert = (kAngstromToMeter * kSToFs) * (kAngstromToMeter * kSToFs) * kAvogadro *
+                                   kDaltonToKg * 1.0E-3;
+// Coulomb energy of two unit charges at 1 A with dielectric 1, in kJ/mol
+constexpr double kCoulombEnergyPerA = kCoulombK * kElectronChargeC * kElectronChargeC / kAngstromToMeter * kAvogadro * 1.0E-3;
+constexpr float kAlip = -0.018f;
+
+// ---- status bits (device -> host) ------------------------------------------------------
+enum : int
+{
+    ST_NONFINITE = 1,       // a position became non-finite
+    ST_PAIR_CAPACITY = 2,   // a pair-list row overflowed
+    ST_CELL_CAPACITY = 4,   // the search grid needs more cells than allocated
+    ST_STALE = 8,           // a particle drifted more than half the list skin: rebuild needed
+};
+
+// particle flag bits (stored as the integer bits of jprm.w)
+enum : uint32_t
+{
+    PF_STATIC = 1u,
+    PF_CHARGED = 2u,
+    PF_HYDROPHOBIC = 4u,
+    PF_RIGID = 8u,
+};
+
+// Device control block: one per simulation handle, in device memory.
+struct Ctl
+{
+    int status;
+    int sbuf;                 // index of the buffer holding the current positions/velocities
+    int lbuf;                 // index of the buffer holding the current particle layout
+    unsigned int done_step;   // last-block counters
+    unsigned int done_bbox;
+    unsigned int done_reorder;
+    long long steps;          // completed steps since setup
+    int max_row;              // largest pair-list row seen at the last build
+    int ncells_needed;
+    // search grid of the current layout (reference formula, nsearch.hpp:342-354)
+    double gmin[3];
+    float gradius;
+    int gnx, gny, gnz;
+    unsigned int bbox_enc[6];  // order-preserving codes of min xyz, max xyz (reset after use)
+    int status_pending;        // bits raised during a step, merged into status by its last block
+    int ext_pending;           // an external force waits in Params::ext
+    double energies[8];       // BS_ENERGY_* of the last evaluation
+};
+
+// Step parameters passed by value to the kernels.
+struct Params
+{
+    int n;                    // particles
+    int npad;                 // n rounded up to a multiple of 32 (ELL row stride)
+    // double-buffered sorted state, indexed by Ctl::sbuf / Ctl::lbuf
+    float4 *pos[2];           // x, y, z, charge
+    float4 *vel[2];           // vx, vy, vz, 0
+    float4 *jprm[2];          // steric a, steric b, hydrophobicity, flags (as bits)
+    int *perm[2];             // sorted slot -> caller id
+    int *inv;                 // caller id -> sorted slot (current layout)
+    float4 *pos_build;        // positions at the last pair-list build (sorted)
+    float4 *iprm[2];          // mass, sasa, transfer, 0 (sorted, re-laid out with jprm)
+    // per-particle data in caller order
+    float4 *ext;              // external force for the next step (caller order)
+    float4 *force_out;        // forces of a force-only evaluation (caller order)
+    // springs: caller-order CSR (static topology)
+    const int *sp_row;        // [n+1]
+    const int *sp_col;        // partner caller id, bit 31 = partner is static
+    const float *sp_k;
+    const float *sp_r0;
+    int sp_maxdeg;
+    // springs: sorted-space ELL, column-major [k * npad + slot]
+    int *se_col;              // partner slot, bit 31 = partner static; -1 = none
+    float *se_k;
+    float *se_r0;
+    int *se_deg;              // [npad]
+    // pair list: ELL column-major [k * npad + slot]
+    int *pl;
+    int *pl_cnt;              // [npad]
+    int pl_cap;
+    // search grid
+    int *cell_of;             // [n] cell of each sorted slot (new layout)
+    int *cell_cnt;            // [cell_cap + 1]
+    int *cell_start;          // [cell_cap + 1]
+    int *cell_fill;           // [cell_cap]
+    int *tmp_perm;            // [n]
+    int cell_cap;
+    // energies: per-block partials
+    double *blk_energy;       // [max_blocks * 8]
+    Ctl *ctl;
+    // configuration
+    float dt;
+    int spring_on, steric_on, coulomb_on, hydro_on, imp_on, visc_on;
+    int steric_mode, dielectric_mode;
+    float c_steric, c_coulomb, c_hydro;       // cutoffs
+    float lo2_s, hi2_s, lo2_c, hi2_c, lo2_h, hi2_h;  // guard bands on r^2
+    float r2_any;             // squared largest cutoff band end (reject above)
+    float list_radius;        // cutoff + skin of the pair list (grid edge)
+    float list_r2;            // squared, slightly inflated
+    float half_skin2;         // (skin/2)^2, slightly deflated
+    float spring_scale, steric_scale, coulomb_scale, hydro_scale, imp_scale;
+    float dielectric;
+    float visc;
+    float imp_z0, imp_alpha;
+    float k_spring_f;         // (float) kSpringForceConvert
+    float k_elec_e;           // kCoulombEnergyPerA
+    float k_elec_f;           // kElecForceConvert / (4 pi)
+    float k_kin;              // kKineticConvert
+    float k_imp_f;            // kImpForceConvert
+    float k_hydro_e;          // N_A * 1e-3
+};
+
+} // namespace bsg

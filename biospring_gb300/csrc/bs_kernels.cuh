@@ -1,0 +1,33 @@
+// bs_kernels.cuh -- kernel declarations of the GB300 step engine.
+#pragma once
+
+#include "bs_common.cuh"
+
+namespace bsg
+{
+
+constexpr int kStepBlock = 128;
+constexpr int kBuildBlock = 128;
+constexpr int kBboxBlock = 256;
+constexpr int kMaxEnergyBlocks = 1 << 16;
+
+// status bits that stop a rebuild; a stale list is what a rebuild repairs
+constexpr int kRebuildBlocking = ST_NONFINITE | ST_PAIR_CAPACITY | ST_CELL_CAPACITY;
+
+enum StepMode
+{
+    MODE_STEP = 0,   // forces + Euler step (SpringNetwork::computeStep)
+    MODE_FORCES = 1, // forces and energies only (SpringNetwork::computeForces)
+};
+
+// Launchers (all asynchronous on `stream`); each returns the number of kernels launched.
+int launch_rebuild(const Params &p, cudaStream_t stream);
+int launch_step(const Params &p, int mode, cudaStream_t stream);
+int launch_unsort(const Params &p, int what, float *out3, cudaStream_t stream);
+int launch_diag_cells(const Params &p, float cutoff, float skin, uint32_t need_flag, long long *out,
+                      cudaStream_t stream);
+int launch_diag_pairs(const Params &p, int term, long long *out, unsigned long long *count,
+                      unsigned long long cap, cudaStream_t stream);
+int launch_set_positions(const Params &p, const float *xyz, const float *vel, cudaStream_t stream);
+
+} // namespace bsg

@@ -1,0 +1,174 @@
+"""Python host mirror of the reference engine's interface, over the C ABI.
+
+Method names follow ``biospring::spn::SpringNetwork`` (src/spn/SpringNetwork.h): particles
+and springs are added first, ``setup`` takes the .msp parameters, then ``computeStep`` /
+``computeForces`` run on the GPU and the getters read the state back. Errors raise
+:class:`BsError` with the library's code and message, where the reference would throw or die.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import BsConfig, BsError, ptr
+
+
+def _f32(a, shape=None):
+    if a is None:
+        return None
+    out = np.ascontiguousarray(a, dtype=np.float32)
+    if shape is not None:
+        out = out.reshape(shape)
+    return out
+
+
+class SpringNetwork:
+    """One simulation handle on the current CUDA device."""
+
+    def __init__(self):
+        self._lib = capi.load()
+        h = C.c_void_p()
+        self._check(self._lib.bs_create(C.byref(h)), None)
+        self._h = h
+        self.n = 0
+        self.config: BsConfig | None = None
+
+    # -- plumbing ---------------------------------------------------------------------
+    def _check(self, rc: int, h=None):
+        if rc != capi.BS_OK:
+            buf = C.create_string_buffer(512)
+            self._lib.bs_last_error(h if h is not None else getattr(self, "_h", None), buf, 512)
+            raise BsError(rc, buf.value.decode(errors="replace"))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.bs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- topology (SpringNetwork::addParticle / addSpring) -------------------------------
+    def addParticles(self, xyz, vel=None, mass=None, charge=None, radius=None, epsilon=None,
+                     hydrophobicity=None, sasa=None, transfer=None, is_static=None):
+        xyz = _f32(xyz, (-1, 3))
+        n = xyz.shape[0]
+        arrs = [_f32(vel, (-1, 3)), _f32(mass), _f32(charge), _f32(radius), _f32(epsilon),
+                _f32(hydrophobicity), _f32(sasa), _f32(transfer)]
+        st = None if is_static is None else np.ascontiguousarray(is_static, dtype=np.uint8)
+        self._keep = (xyz, arrs, st)
+        self._check(self._lib.bs_upload_particles(
+            self._h, n, ptr(xyz, C.c_float), *[ptr(a, C.c_float) for a in arrs], ptr(st, C.c_uint8)), self._h)
+        self.n += n
+
+    def addSprings(self, ij, equilibrium, stiffness):
+        ij = np.ascontiguousarray(ij, dtype=np.int32).reshape(-1, 2)
+        r0 = _f32(equilibrium)
+        k = _f32(stiffness)
+        self._check(self._lib.bs_upload_springs(self._h, ij.shape[0], ptr(ij, C.c_int32), ptr(r0, C.c_float),
+                                                ptr(k, C.c_float)), self._h)
+
+    def setRigidBodies(self, bodies):
+        offsets = np.zeros(len(bodies) + 1, dtype=np.int32)
+        for b, ids in enumerate(bodies):
+            offsets[b + 1] = offsets[b] + len(ids)
+        ids = np.ascontiguousarray(np.concatenate([np.asarray(b, dtype=np.int32) for b in bodies])
+                                   if bodies else np.zeros(0, np.int32), dtype=np.int32)
+        self._check(self._lib.bs_set_rigid_bodies(self._h, len(bodies), ptr(offsets, C.c_int32),
+                                                  ptr(ids, C.c_int32)), self._h)
+
+    # -- setup and run --------------------------------------------------------------------
+    def setup(self, config):
+        if isinstance(config, dict):
+            cfg = capi.default_config()
+            for k, v in config.items():
+                setattr(cfg, k, v)
+            config = cfg
+        self.config = config
+        self._check(self._lib.bs_setup(self._h, C.byref(config)), self._h)
+
+    def computeStep(self, nsteps: int = 1):
+        self._check(self._lib.bs_step(self._h, int(nsteps)), self._h)
+
+    def computeForces(self):
+        self._check(self._lib.bs_compute_forces(self._h), self._h)
+
+    # -- state ------------------------------------------------------------------------------
+    def _get3(self, fn):
+        out = np.empty((self.n, 3), dtype=np.float32)
+        self._check(fn(self._h, ptr(out, C.c_float)), self._h)
+        return out
+
+    def getPositions(self):
+        return self._get3(self._lib.bs_get_positions)
+
+    def getVelocities(self):
+        return self._get3(self._lib.bs_get_velocities)
+
+    def getForces(self):
+        return self._get3(self._lib.bs_get_forces)
+
+    def setPositions(self, xyz):
+        xyz = _f32(xyz, (-1, 3))
+        self._check(self._lib.bs_set_positions(self._h, ptr(xyz, C.c_float)), self._h)
+
+    def setVelocities(self, vel):
+        vel = _f32(vel, (-1, 3))
+        self._check(self._lib.bs_set_velocities(self._h, ptr(vel, C.c_float)), self._h)
+
+    def setForce(self, i: int, f):
+        f = _f32(f)
+        self._check(self._lib.bs_set_force(self._h, int(i), ptr(f, C.c_float)), self._h)
+
+    def energies(self) -> dict:
+        out = np.zeros(6, dtype=np.float64)
+        self._check(self._lib.bs_get_energies(self._h, ptr(out, C.c_double)), self._h)
+        return dict(zip(capi.ENERGY_NAMES, out.tolist()))
+
+    def getKineticEnergy(self):
+        return self.energies()["kinetic"]
+
+    def getSpringEnergy(self):
+        return self.energies()["spring"]
+
+    def getStericEnergy(self):
+        return self.energies()["steric"]
+
+    def getElectrostaticEnergy(self):
+        return self.energies()["electrostatic"]
+
+    def getIMPEnergy(self):
+        return self.energies()["imp"]
+
+    def getHydrophobicEnergy(self):
+        return self.energies()["hydrophobic"]
+
+    # -- diagnostics ------------------------------------------------------------------------
+    def getPairs(self, term: int) -> np.ndarray:
+        n = C.c_int64()
+        self._check(self._lib.bs_get_pairs(self._h, term, None, 0, C.byref(n)), self._h)
+        out = np.zeros((max(n.value, 1), 2), dtype=np.int64)
+        self._check(self._lib.bs_get_pairs(self._h, term, ptr(out, C.c_int64), n.value, C.byref(n)), self._h)
+        return out[: n.value]
+
+    def getCells(self, term: int) -> np.ndarray:
+        out = np.zeros(self.n, dtype=np.int64)
+        self._check(self._lib.bs_get_cells(self._h, term, ptr(out, C.c_int64)), self._h)
+        return out
+
+    def launchCount(self) -> int:
+        c = C.c_int64()
+        self._check(self._lib.bs_get_launch_count(self._h, C.byref(c)), self._h)
+        return c.value

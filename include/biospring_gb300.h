@@ -1,0 +1,206 @@
+/*
+ * biospring_gb300.h -- C ABI of the GB300 (sm_103a) implementation of BioSpring's
+ * per-step force-and-integrate loop.
+ *
+ * The reference engine is the C++ class biospring::spn::SpringNetwork
+ * (src/spn/SpringNetwork.h). A CUDA backend plugs into it the same way the
+ * OpenCL backend does (src/opencl/SpringNetworkOpenCL.h:84-182): a subclass that
+ * overrides the step virtuals and forwards them to these entry points.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: BS_OK (0) or one of BS_E_*.
+ *     Nothing aborts the process; bs_last_error() gives a one-line reason.
+ *   - Arrays are plain host pointers, structure-of-arrays, in the caller's
+ *     particle order (the reference's particle index). They are copied on call.
+ *   - Positions, velocities and forces are float[3*n] (x0,y0,z0,x1,...).
+ *   - Units are the reference's: Angstrom, femtosecond, Dalton, kJ/mol,
+ *     forces in Da.A.fs^-2 (src/forcefield/constants.hpp:88-118).
+ *   - A handle is not thread-safe; several handles may coexist. Each handle owns
+ *     one CUDA stream on the current device.
+ */
+#ifndef BIOSPRING_GB300_H
+#define BIOSPRING_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------ */
+#define BS_OK 0
+#define BS_E_ARG 1        /* invalid argument (reference: std::invalid_argument / out_of_range) */
+#define BS_E_CUDA 2       /* a CUDA runtime call failed */
+#define BS_E_NONFINITE 3  /* non-finite position (reference: logging::die, SpringNetwork.cpp:222-229) */
+#define BS_E_CAPACITY 4   /* a device list overflowed and could not be regrown */
+#define BS_E_TIMEOUT 5    /* a bounded device-side wait gave up */
+#define BS_E_STATE 6      /* call made in the wrong order (e.g. step before setup) */
+
+/* ---- steric modes (steric.mode, src/configuration/Setting.hpp:269-273) ---------- */
+#define BS_STERIC_LINEAR 0            /* "linear" */
+#define BS_STERIC_LJ_12_6_AMBER 1     /* "lennard-jones-12-6Amber" */
+#define BS_STERIC_LJ_8_6_LEWITT 2     /* "lennard-jones-8-6Lewitt" */
+#define BS_STERIC_LJ_8_6_ZACHARIAS 3  /* "lennard-jones-8-6Zacharias" */
+
+/* ---- dielectric modes (extension; the reference only has a constant) ------------ */
+#define BS_DIELECTRIC_CONSTANT 0  /* eps = coulomb.dielectric (energy/electrostatic.hpp:16-49) */
+#define BS_DIELECTRIC_DISTANCE 1  /* eps = coulomb.dielectric * r  (no counterpart in the reference) */
+
+/* ---- nonbonded terms, for the pair/cell diagnostics ---------------------------- */
+#define BS_TERM_STERIC 0
+#define BS_TERM_COULOMB 1
+#define BS_TERM_HYDROPHOBIC 2
+
+/* ---- energies, order of bs_get_energies() -------------------------------------- */
+#define BS_ENERGY_KINETIC 0
+#define BS_ENERGY_SPRING 1
+#define BS_ENERGY_STERIC 2
+#define BS_ENERGY_ELECTROSTATIC 3
+#define BS_ENERGY_IMP 4
+#define BS_ENERGY_HYDROPHOBIC 5
+#define BS_NUM_ENERGIES 6
+
+/*
+ * Run parameters: a plain mirror of the .msp groups the step reads
+ * (src/configuration/Configuration.hpp:18-151, defaults at :153-234), plus a
+ * few device-path knobs grouped last. bs_default_config() fills it exactly
+ * like defaultConfiguration() (Configuration.hpp:153).
+ */
+typedef struct bs_config {
+    /* simulation.* */
+    int32_t nbsteps;
+    double timestep;        /* fs */
+    double neighborskin;    /* A; reference cell-list skin (nsearch.hpp:185-190) */
+    /* spring.* */
+    int32_t spring_enable;
+    double spring_scale;
+    /* steric.* */
+    int32_t steric_enable;
+    double steric_gridscale;
+    double steric_cutoff;
+    int32_t steric_mode;    /* BS_STERIC_* */
+    /* coulomb.* */
+    int32_t coulomb_enable;
+    double coulomb_scale;
+    double coulomb_cutoff;
+    double coulomb_dielectric;
+    /* hydrophobicity.* */
+    int32_t hydrophobicity_enable;
+    double hydrophobicity_scale;
+    double hydrophobicity_cutoff;
+    /* impala.* */
+    int32_t impala_enable;
+    double impala_scale;
+    /* viscosity.* */
+    int32_t viscosity_enable;
+    double viscosity_value; /* Da/fs */
+    /* rigidbody.enable */
+    int32_t rigidbody_enable;
+    /* --- device-path knobs (new .msp group "cuda.*"; no reference counterpart) --- */
+    int32_t dielectric_mode;  /* BS_DIELECTRIC_* */
+    double impala_z0;         /* membrane half-thickness, reference hard-codes 15.75 (imp.hpp:13-15) */
+    double impala_alpha;      /* reference hard-codes 1.99 */
+    int32_t rebuild_every;    /* rebuild the device pair list every K steps (>= 1) */
+    double list_skin;         /* A; extra radius of the device pair list; drift > skin/2 forces a rebuild */
+} bs_config;
+
+typedef struct bs_sim bs_sim;
+
+/* Fills *cfg like configuration::defaultConfiguration() (Configuration.hpp:153-234)
+ * and sets the device knobs to dielectric_mode=constant, impala_z0=15.75,
+ * impala_alpha=1.99, rebuild_every=10, list_skin=1.0. */
+int bs_default_config(bs_config *cfg);
+
+/* Parses .msp text ("group.param = value" lines, '#' comments) on top of *cfg.
+ * Unknown or duplicated parameters are rejected, as in
+ * SafeConfigurationReader::read (src/configuration/SafeConfigurationReader.cpp:11-40).
+ * err (nullable) receives a one-line message on failure. */
+int bs_config_parse_msp(const char *text, bs_config *cfg, char *err, size_t err_len);
+
+/* Creates an empty simulation on the current CUDA device
+ * (replaces SpringNetwork::SpringNetwork(), SpringNetwork.h:103). */
+int bs_create(bs_sim **out);
+
+/* Frees every device and host resource of the handle (SpringNetwork::~SpringNetwork). */
+int bs_destroy(bs_sim *sim);
+
+/* Copies n particles in (replaces SpringNetwork::addParticle, SpringNetwork.cpp:498-527,
+ * called n times in index order). Nullable arrays take the ParticleProperty defaults
+ * (src/spn/ParticleProperty.h:20-24): vel 0, mass 1, charge 0, radius 1, epsilon 0,
+ * hydrophobicity 0, sasa 0, transfer 0, is_static 0. A particle is charged iff
+ * charge != 0 and hydrophobic iff hydrophobicity != 0 (ParticleProperty.cpp). */
+int bs_upload_particles(bs_sim *sim, int64_t n, const float *xyz, const float *vel,
+                        const float *mass, const float *charge, const float *radius,
+                        const float *epsilon, const float *hydrophobicity,
+                        const float *sasa, const float *transfer, const uint8_t *is_static);
+
+/* Adds s springs (replaces s calls of SpringNetwork::addSpring(id1, id2, equilibrium,
+ * stiffness), SpringNetwork.cpp:452-486): out-of-range ids and id1 == id2 are
+ * BS_E_ARG; a spring between an already-bonded pair is ignored. Springs also
+ * exclude their pair from every nonbonded term when spring.enable is set
+ * (Particle.cpp:213-218). ij is int32[2*s]. */
+int bs_upload_springs(bs_sim *sim, int64_t s, const int32_t *ij, const float *equilibrium,
+                      const float *stiffness);
+
+/* Declares rigid bodies: body b owns ids[offsets[b] .. offsets[b+1]-1].
+ * Replaces RigidBodiesManager::InitRigidBodies (RigidBodiesManager.cpp:11-43);
+ * springs whose two ends are rigid stop acting (RigidBody.cpp:41-53).
+ * Effective when rigidbody_enable is set. */
+int bs_set_rigid_bodies(bs_sim *sim, int32_t nbodies, const int32_t *offsets, const int32_t *ids);
+
+/* Validates the configuration, uploads everything and builds the first cell list
+ * and pair list (replaces SpringNetwork::setup, SpringNetwork.cpp:646-737).
+ * Cutoffs below 1e-6 for an enabled term are BS_E_ARG (SpringNetwork.cpp:667-668). */
+int bs_setup(bs_sim *sim, const bs_config *cfg);
+
+/* Runs nsteps full steps (replaces nsteps calls of SpringNetwork::computeStep,
+ * SpringNetwork.cpp:251-268). Energies of the last step are kept for
+ * bs_get_energies. Returns BS_E_NONFINITE if a position became non-finite. */
+int bs_step(bs_sim *sim, int32_t nsteps);
+
+/* Computes forces and energies at the current positions without integrating
+ * (replaces idleRun() + computeForces(), SpringNetwork.cpp:244-249, 344-365).
+ * The forces are then readable with bs_get_forces. */
+int bs_compute_forces(bs_sim *sim);
+
+/* Reads or overwrites per-particle state, in the caller's particle order
+ * (Particle::getPosition / setPosition ...). Setting positions or velocities
+ * invalidates the pair list, which is rebuilt before the next force evaluation. */
+int bs_get_positions(bs_sim *sim, float *xyz);
+int bs_get_velocities(bs_sim *sim, float *vel);
+int bs_get_forces(bs_sim *sim, float *f);
+int bs_set_positions(bs_sim *sim, const float *xyz);
+int bs_set_velocities(bs_sim *sim, const float *vel);
+
+/* Adds an external force to particle i for the next step only (replaces
+ * SpringNetwork::setForce, SpringNetwork.cpp:438-442, the interactor path). */
+int bs_set_force(bs_sim *sim, int64_t i, const float f[3]);
+
+/* Energies of the last step or force evaluation, BS_ENERGY_* order, in kJ/mol
+ * (SpringNetwork::getKineticEnergy ... getHydrophobicEnergy, SpringNetwork.h:157-162).
+ * They are reduced in FP64 on the device. */
+int bs_get_energies(bs_sim *sim, double out[BS_NUM_ENERGIES]);
+
+/* Diagnostics for the bit-exact checks.
+ * bs_get_pairs: the unique interacting pairs (i < j, caller ids) of one nonbonded term
+ * at the current positions, i.e. the pairs for which the reference calls the force
+ * routine (Particle.cpp:191-253, 269-330, 368-429). Sorted by (i, j). If *n_out > cap
+ * only cap pairs are written. out is int64[2*cap].
+ * bs_get_cells: the reference cell id (nsearch.hpp:277-293) of every particle for the
+ * grid of one term (cell edge = cutoff + neighborskin, bounding box of all particles),
+ * computed on the device; -1 for particles not in that grid. */
+int bs_get_pairs(bs_sim *sim, int32_t term, int64_t *out, int64_t cap, int64_t *n_out);
+int bs_get_cells(bs_sim *sim, int32_t term, int64_t *out);
+
+/* Number of kernels this handle launched so far (for launch accounting). */
+int bs_get_launch_count(bs_sim *sim, int64_t *count);
+
+/* Copies the last error message of the handle (or of the library when sim is NULL). */
+int bs_last_error(bs_sim *sim, char *buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BIOSPRING_GB300_H */

@@ -1,0 +1,211 @@
+"""TEST INFRASTRUCTURE: ctypes access to the CPU oracle and to the compiled reference.
+
+* ``Oracle``    -- the CPU restatement in oracle/bs_oracle.cpp (libbs_oracle.so), built on
+  any machine by :func:`build_oracle`.
+* ``Reference`` -- the unmodified reference engine compiled from its sources by oracle/ref.mk
+  into oracle/_ref/libbsref.so; only present where the reference sources are.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module, and
+only as the checker or the timed CPU baseline, never as the product path.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "libbs_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libbsref.so")
+
+
+def build_oracle() -> str:
+    src = os.path.join(HERE, "bs_oracle.cpp")
+    hdr = os.path.join(os.path.dirname(HERE), "include", "biospring_gb300.h")
+    if (not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < max(os.path.getmtime(src),
+                                                                           os.path.getmtime(hdr))):
+        subprocess.run(["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", src,
+                        "-o", ORACLE_SO], check=True)
+    return ORACLE_SO
+
+
+def build_reference() -> str | None:
+    """Builds oracle/_ref/libbsref.so when the reference sources are present (make -f oracle/ref.mk)."""
+    proc = subprocess.run(["make", "-s", "-f", os.path.join(HERE, "ref.mk"), f"-j{os.cpu_count() or 4}"],
+                          cwd=os.path.dirname(HERE), stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("reference build failed:\n" + proc.stdout[-4000:])
+    return REF_SO if os.path.exists(REF_SO) else None
+
+
+def have_reference() -> bool:
+    return os.path.exists(REF_SO)
+
+
+_f32p = C.POINTER(C.c_float)
+_i32p = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+_u8p = C.POINTER(C.c_uint8)
+_f64p = C.POINTER(C.c_double)
+
+
+def _bind(lib, prefix: str, cfg_type):
+    sig = {
+        "create": (C.c_void_p, [C.POINTER(cfg_type), C.c_int64, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
+                                _f32p, _f32p, _u8p, C.c_int64, _i32p, _f32p, _f32p]),
+        "destroy": (None, [C.c_void_p]),
+        "step": (C.c_int, [C.c_void_p, C.c_int32]),
+        "time_steps": (C.c_double, [C.c_void_p, C.c_int32]),
+        "compute_forces": (C.c_int, [C.c_void_p]),
+        "get_positions": (None, [C.c_void_p, _f32p]),
+        "get_velocities": (None, [C.c_void_p, _f32p]),
+        "get_forces": (None, [C.c_void_p, _f32p]),
+        "set_positions": (None, [C.c_void_p, _f32p]),
+        "get_energies": (None, [C.c_void_p, _f64p]),
+        "get_pairs": (C.c_int64, [C.c_void_p, C.c_int32, _i64p, C.c_int64]),
+        "get_cells": (C.c_int, [C.c_void_p, C.c_int32, _i64p]),
+    }
+    if prefix == "bso_":
+        sig["set_rigid_bodies"] = (C.c_int, [C.c_void_p, C.c_int32, _i32p, _i32p])
+        sig["set_velocities"] = (None, [C.c_void_p, _f32p])
+        sig["eval_fp64"] = (C.c_int, [C.c_void_p, _f64p, _f64p])
+    fns = {}
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, prefix + name)
+        fn.restype = res
+        fn.argtypes = args
+        fns[name] = fn
+    return fns
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+class _CpuSim:
+    _lib = None
+    _fns = None
+    PREFIX = ""
+    PATH = ""
+
+    @classmethod
+    def _load(cls):
+        from biospring_gb300.capi import BsConfig
+        if cls._fns is None:
+            if not os.path.exists(cls.PATH):
+                raise RuntimeError(f"{cls.PATH} is missing")
+            cls._lib = C.CDLL(cls.PATH)
+            cls._fns = _bind(cls._lib, cls.PREFIX, BsConfig)
+        return cls._fns
+
+    def __init__(self, system, cfg=None):
+        f = self._load()
+        cfg = system.bs_config() if cfg is None else cfg
+        self.cfg = cfg
+        a = {k: (None if v is None else np.ascontiguousarray(v)) for k, v in system.arrays().items()}
+        self._keep = a
+        xyz = np.ascontiguousarray(a["xyz"], np.float32)
+        f32 = lambda k: None if a[k] is None else np.ascontiguousarray(a[k], np.float32)  # noqa: E731
+        self._arr = [xyz] + [f32(k) for k in ("vel", "mass", "charge", "radius", "epsilon", "hydrophobicity",
+                                              "sasa", "transfer")]
+        st = None if a["is_static"] is None else np.ascontiguousarray(a["is_static"], np.uint8)
+        self._st = st
+        ij = np.ascontiguousarray(system.ij, np.int32)
+        r0 = np.ascontiguousarray(system.r0, np.float32)
+        k = np.ascontiguousarray(system.k, np.float32)
+        self._sp = (ij, r0, k)
+        self.n = system.n
+        self.h = f["create"](C.byref(cfg), self.n, *[_p(x, C.c_float) for x in self._arr], _p(st, C.c_uint8),
+                             ij.shape[0], _p(ij, C.c_int32), _p(r0, C.c_float), _p(k, C.c_float))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._fns["destroy"](self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, n=1):
+        rc = self._fns["step"](self.h, int(n))
+        if rc != 0:
+            raise RuntimeError(f"oracle step failed with code {rc}")
+
+    def time_steps(self, n):
+        return self._fns["time_steps"](self.h, int(n))
+
+    def compute_forces(self):
+        self._fns["compute_forces"](self.h)
+
+    def _get3(self, name):
+        out = np.zeros((self.n, 3), np.float32)
+        self._fns[name](self.h, _p(out, C.c_float))
+        return out
+
+    def positions(self):
+        return self._get3("get_positions")
+
+    def velocities(self):
+        return self._get3("get_velocities")
+
+    def forces(self):
+        return self._get3("get_forces")
+
+    def set_positions(self, xyz):
+        xyz = np.ascontiguousarray(xyz, np.float32)
+        self._fns["set_positions"](self.h, _p(xyz, C.c_float))
+
+    def energies(self):
+        out = np.zeros(6, np.float64)
+        self._fns["get_energies"](self.h, _p(out, C.c_double))
+        return out
+
+    def pairs(self, term):
+        n = self._fns["get_pairs"](self.h, term, None, 0)
+        out = np.zeros((max(n, 1), 2), np.int64)
+        self._fns["get_pairs"](self.h, term, _p(out, C.c_int64), n)
+        out = out[:n]
+        return out[np.lexsort((out[:, 1], out[:, 0]))]
+
+    def cells(self, term):
+        out = np.zeros(self.n, np.int64)
+        self._fns["get_cells"](self.h, term, _p(out, C.c_int64))
+        return out
+
+
+class Oracle(_CpuSim):
+    PREFIX = "bso_"
+    PATH = ORACLE_SO
+
+    def __init__(self, system, cfg=None):
+        super().__init__(system, cfg)
+        if system.bodies and self.cfg.rigidbody_enable:
+            self.set_rigid_bodies(system.bodies)
+
+    def set_rigid_bodies(self, bodies):
+        offsets = np.zeros(len(bodies) + 1, np.int32)
+        for b, ids in enumerate(bodies):
+            offsets[b + 1] = offsets[b] + len(ids)
+        ids = np.ascontiguousarray(np.concatenate([np.asarray(b, np.int32) for b in bodies]), np.int32)
+        self._fns["set_rigid_bodies"](self.h, len(bodies), _p(offsets, C.c_int32), _p(ids, C.c_int32))
+
+    def set_velocities(self, v):
+        v = np.ascontiguousarray(v, np.float32)
+        self._fns["set_velocities"](self.h, _p(v, C.c_float))
+
+    def eval_fp64(self):
+        f = np.zeros((self.n, 3), np.float64)
+        e = np.zeros(6, np.float64)
+        self._fns["eval_fp64"](self.h, _p(f, C.c_double), _p(e, C.c_double))
+        return f, e
+
+
+class Reference(_CpuSim):
+    PREFIX = "bsref_"
+    PATH = REF_SO

@@ -1,0 +1,343 @@
+"""Benchmark of BioSpring's per-step force-and-integrate loop on GB300.
+
+Workload (one "step" = one simulation step of the whole system): 100,000 particles filled
+uniformly (minimum separation 3 A) in a 160 A cube, springs below 5 A (mean degree ~11.3,
+stiffness log-uniform in [0.1, 10] kJ/mol/A^2), 20% charged +-1, Coulomb with the
+distance-dependent dielectric eps = 4 r and Amber 12-6 LJ (eps 0.2 kcal/mol, r 3.5 A), both
+cut at 12 A, pair list rebuilt every 10 steps. Synthetic, seeded (no dataset).
+
+Native arm: inputs resident in HBM; before every timed step L2 is flushed (a 256 MB write,
+untimed); each step (the rebuild every 10th step, then the step kernel) is bracketed by CUDA
+events on the library's stream. ``e2e`` drives the same steps through the C ABI with host
+buffers: per step, external forces H2D from pinned memory, one bs_step call, energies D2H.
+
+Reference arm (--impl reference): the CPU restatement of the reference's step (the reference
+itself cannot be built where the sources are absent) timed on all host cores with OpenMP.
+
+Prints one JSON line.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s (100k-particle plain step)"
+UNIT = "particle-steps/s"
+N_PARTICLES = 100_000
+BOX = 160.0
+REBUILD = 10
+STEP_BYTES_PER_PARTICLE_BASE = 84.0   # positions r+w 32, velocities r+w 32, parameters 16, row pointer 4
+SPRING_BYTES_PER_ENTRY = 12.0         # partner index + stiffness + rest length
+REBUILD_BYTES_PER_PARTICLE = 104.0    # key 4 + permutation 4 + gather/scatter of x, v, parameters 3 x 32
+
+
+def peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(seed: int = 42):
+    from biospring_gb300 import workloads as W
+    return W.uniform_lj(n=N_PARTICLES, box=BOX, seed=seed, dielectric_mode=1, rebuild_every=REBUILD,
+                        list_skin=0.5)
+
+
+def algorithmic(system, net) -> dict:
+    """Algorithmic bytes and FLOPs of one step kernel launch (counts of unique interactions)."""
+    n = system.n
+    s = system.ij.shape[0]
+    dbar = 2.0 * s / n
+    pairs_lj = int(net.getPairs(0).shape[0])
+    pairs_q = int(net.getPairs(1).shape[0])
+    step_bytes = n * (STEP_BYTES_PER_PARTICLE_BASE + SPRING_BYTES_PER_ENTRY * dbar)
+    flops = 30.0 * pairs_lj + 12.0 * pairs_q + 24.0 * s + 23.0 * n
+    return {"mean_spring_degree": dbar, "unique_lj_pairs": pairs_lj, "unique_coulomb_pairs": pairs_q,
+            "step_kernel_bytes": step_bytes, "step_flops": flops,
+            "bytes_per_particle_step": step_bytes / n + REBUILD_BYTES_PER_PARTICLE / REBUILD}
+
+
+def run_native(args) -> dict:
+    import torch
+    from biospring_gb300 import SpringNetwork
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    system = make_workload(seed=42 + rank)
+    net = SpringNetwork()
+    net.addParticles(**{k: v for k, v in system.arrays().items() if v is not None})
+    net.addSprings(system.ij, system.r0, system.k)
+    net.setup(system.bs_config())
+    stream = torch.cuda.ExternalStream(net.stream())
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    # warm-up: full graph-captured periods plus the timed loop's launch pattern
+    net.computeStep(max(args.warmup, 3) * REBUILD)
+    alg = algorithmic(system, net)
+
+    steps = args.steps
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    launches0 = net.launchCount()
+    step0 = net.stepCount()
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for i in range(steps):
+            flush.zero_()  # evict L2 (untimed: before the start event)
+            ev[i][0].record(stream)
+            if i % REBUILD == 0:
+                net.launchPhase(0)
+            ev[i][1].record(stream)
+            net.launchPhase(1)
+            ev[i][2].record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clocks = sampler.stop()
+    net.synchronize()
+    done = net.stepCount() - step0
+    launches = net.launchCount() - launches0
+    if done != steps:
+        raise RuntimeError(f"timed region completed {done} of {steps} steps (a stale list forced a redo)")
+    step_ms = [ev[i][0].elapsed_time(ev[i][2]) for i in range(steps)]
+    kern_ms = [ev[i][1].elapsed_time(ev[i][2]) for i in range(steps)]
+    total_ms = float(sum(step_ms))
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * system.n * steps / (total_ms * 1e-3)
+
+    # warm, continuous throughput (graph-captured periods, no flush), for context
+    torch.cuda.synchronize()
+    w0 = torch.cuda.Event(enable_timing=True)
+    w1 = torch.cuda.Event(enable_timing=True)
+    net.synchronize()
+    w0.record(stream)
+    net.computeStepAsync(10 * REBUILD)
+    w1.record(stream)
+    net.synchronize()
+    warm_ms = w0.elapsed_time(w1)
+
+    # end to end through the C ABI with host buffers
+    ext = torch.zeros((system.n, 3), dtype=torch.float32).pin_memory().numpy()
+    e2e_steps = max(steps, 20)
+    for _ in range(3):
+        net.setExternalForces(ext)
+        net.computeStep(1)
+        net.energies()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        net.setExternalForces(ext)
+        net.computeStep(1)
+        net.energies()
+    t1 = time.perf_counter()
+    e2e_value = world * system.n * e2e_steps / (t1 - t0)
+
+    pk = peaks()
+    kernel_s = statistics.mean(kern_ms) * 1e-3
+    achieved = alg["step_kernel_bytes"] / kernel_s / 1e9
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded uniform fill, springs, charges)",
+        "config": {
+            "workload": f"uniform_lj_100k: N={system.n}, cube {BOX:g} A, springs<5A (mean degree "
+                        f"{alg['mean_spring_degree']:.2f}), 20% charged, Coulomb eps=4r 12 A, LJ 12-6 Amber 12 A, "
+                        f"rebuild every {REBUILD} steps, list skin 0.5 A",
+            "global_batch": system.n * world,
+            "parallelism": f"replicas{world}" if world > 1 else "single",
+            "l2": "flushed (256 MB write) before every timed step",
+            "timing": "CUDA events on the library stream around each step (rebuild on every 10th)",
+        },
+        "gpu_launches": int(launches),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(system.n * 16),
+                "d2h_bytes_per_step": 48,
+                "path": "bs_set_external_forces + bs_step(1) + bs_get_energies per step"},
+        "roofline": {
+            "bound": "hbm",
+            "kernel": "k_step (forces + Euler step)",
+            "achieved": achieved,
+            "peak": pk["hbm_gbs"],
+            "unit": "GB/s",
+            "frac": achieved / pk["hbm_gbs"],
+            "traffic": None,
+            "peak_src": pk["src"],
+            "algorithmic_bytes_per_launch": alg["step_kernel_bytes"],
+            "kernel_ms": kernel_s * 1e3,
+            "flops_per_step": alg["step_flops"],
+            "fp32_tflops": alg["step_flops"] / kernel_s / 1e12,
+        },
+        "warm_continuous": {"value": system.n * 10 * REBUILD / (warm_ms * 1e-3), "unit": UNIT,
+                            "ms_per_step": warm_ms / (10 * REBUILD)},
+        "clocks": clocks,
+        "interactions": {k: alg[k] for k in ("unique_lj_pairs", "unique_coulomb_pairs")},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(system, seconds=args.cpu_seconds)
+    net.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def cpu_baseline(system, seconds: float = 15.0) -> dict:
+    """The CPU restatement of the reference step on all host cores (OpenMP), bounded sample."""
+    from oracle import pyoracle
+    pyoracle.build_oracle()
+    cores = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(cores)
+    orc = pyoracle.Oracle(system)
+    orc.time_steps(1)
+    t = orc.time_steps(1)
+    nsteps = max(1, min(30, int(seconds / max(t, 1e-3))))
+    t = orc.time_steps(nsteps)
+    orc.close()
+    return {"value": system.n * nsteps / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{nsteps} full steps of the 100k workload after 2 untimed ones"}
+
+
+def run_reference(args) -> dict | None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    from oracle import pyoracle
+    pyoracle.build_oracle()
+    cores = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(cores)
+    system = make_workload(seed=42)
+    orc = pyoracle.Oracle(system)
+    for _ in range(args.warmup):
+        orc.time_steps(1)
+    t = orc.time_steps(args.steps)
+    orc.close()
+    value = system.n * args.steps / t
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": "uniform_lj_100k (same system as the native arm)", "global_batch": system.n},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full steps after {args.warmup} warm-up steps, OpenMP on all cores"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        if args.steps > 20:
+            args.steps = 10  # a bounded CPU sample (each step is ~1 s of CPU work)
+        args.warmup = max(1, min(args.warmup, 3))
+        out = run_reference(args)
+    else:
+        args.warmup = max(args.warmup, 3)
+        from biospring_gb300 import build
+        if not os.path.exists(build.LIB):
+            build.build_all()
+        out = run_native(args)
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

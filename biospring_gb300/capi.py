@@ -97,6 +97,11 @@ SIGNATURES = {
     "bs_set_rigid_bodies": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _i32p]),
     "bs_setup": (C.c_int, [C.c_void_p, C.POINTER(BsConfig)]),
     "bs_step": (C.c_int, [C.c_void_p, C.c_int32]),
+    "bs_step_async": (C.c_int, [C.c_void_p, C.c_int32]),
+    "bs_synchronize": (C.c_int, [C.c_void_p]),
+    "bs_get_step_count": (C.c_int, [C.c_void_p, _i64p]),
+    "bs_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "bs_launch_phase": (C.c_int, [C.c_void_p, C.c_int32]),
     "bs_compute_forces": (C.c_int, [C.c_void_p]),
     "bs_get_positions": (C.c_int, [C.c_void_p, _f32p]),
     "bs_get_velocities": (C.c_int, [C.c_void_p, _f32p]),
@@ -104,6 +109,7 @@ SIGNATURES = {
     "bs_set_positions": (C.c_int, [C.c_void_p, _f32p]),
     "bs_set_velocities": (C.c_int, [C.c_void_p, _f32p]),
     "bs_set_force": (C.c_int, [C.c_void_p, C.c_int64, _f32p]),
+    "bs_set_external_forces": (C.c_int, [C.c_void_p, _f32p]),
     "bs_get_energies": (C.c_int, [C.c_void_p, _f64p]),
     "bs_get_pairs": (C.c_int, [C.c_void_p, C.c_int32, _i64p, C.c_int64, _i64p]),
     "bs_get_cells": (C.c_int, [C.c_void_p, C.c_int32, _i64p]),

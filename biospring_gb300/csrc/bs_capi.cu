@@ -70,6 +70,7 @@ struct bs_sim
     bool list_valid = false;
     int since_rebuild = 0;
     long long steps_done = 0;
+    long long target = 0; // steps requested since setup
     cudaGraphExec_t period_graph = nullptr;
     int period_kernels = 0;
     long long launches = 0;
@@ -116,6 +117,10 @@ void release_device(bs_sim *s)
 {
     destroy_graph(s);
     s->dev.free_all();
+    s->diag_out = nullptr;
+    s->diag_count = nullptr;
+    s->diag_cap = 0;
+    s->staging = nullptr;
     if (s->ctl_host)
     {
         cudaFreeHost(s->ctl_host);
@@ -183,6 +188,7 @@ int sync_ext(bs_sim *s)
     BS_CUDA(cudaStreamSynchronize(s->stream));
     std::memset(s->ext_host, 0, sizeof(float4) * s->n);
     s->ext_dirty = false;
+    // (the pinned buffer is reused for the next step's forces once the copy has completed)
     return BS_OK;
 }
 
@@ -655,6 +661,7 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
 
     s->ready = true;
     s->steps_done = 0;
+    s->target = 0;
     s->list_valid = false;
     rc = rebuild_now(s);
     if (rc)
@@ -665,7 +672,46 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     return BS_OK;
 }
 
-int bs_step(bs_sim *s, int32_t nsteps)
+// Enqueues `count` steps following the rebuild schedule (a rebuild every K steps, or when
+// the list is invalid); aligned periods go out as one captured graph.
+static int enqueue_steps(bs_sim *s, long long count)
+{
+    const int K = std::max(1, s->cfg.rebuild_every);
+    long long remaining = count;
+    while (remaining > 0)
+    {
+        if (!s->list_valid || s->since_rebuild >= K)
+        {
+            if (remaining >= K)
+            {
+                if (!s->period_graph)
+                {
+                    const int rc = capture_period_graph(s);
+                    if (rc)
+                        return rc;
+                }
+                BS_CUDA(cudaGraphLaunch(s->period_graph, s->stream));
+                s->launches += s->period_kernels;
+                s->list_valid = true;
+                s->since_rebuild = K;
+                remaining -= K;
+                continue;
+            }
+            s->launches += launch_rebuild(s->p, s->stream);
+            s->list_valid = true;
+            s->since_rebuild = 0;
+        }
+        const long long chunk = std::min<long long>(remaining, K - s->since_rebuild);
+        for (long long k = 0; k < chunk; ++k)
+            s->launches += launch_step(s->p, MODE_STEP, s->stream);
+        s->since_rebuild += static_cast<int>(chunk);
+        remaining -= chunk;
+    }
+    BS_CUDA(cudaGetLastError());
+    return BS_OK;
+}
+
+int bs_step_async(bs_sim *s, int32_t nsteps)
 {
     if (!s)
         return fail(nullptr, BS_E_ARG, "null handle");
@@ -676,45 +722,19 @@ int bs_step(bs_sim *s, int32_t nsteps)
     int rc = sync_ext(s);
     if (rc)
         return rc;
-    const int K = std::max(1, s->cfg.rebuild_every);
-    const long long target = s->steps_done + nsteps;
-    for (int round = 0; round < 64 && s->steps_done < target; ++round)
+    s->target += nsteps;
+    return enqueue_steps(s, nsteps);
+}
+
+int bs_synchronize(bs_sim *s)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    for (int round = 0; round < 64; ++round)
     {
-        long long remaining = target - s->steps_done;
-        long long queued = 0;
-        while (remaining > 0)
-        {
-            if (!s->list_valid || s->since_rebuild >= K)
-            {
-                if (remaining >= K)
-                {
-                    if (!s->period_graph)
-                    {
-                        rc = capture_period_graph(s);
-                        if (rc)
-                            return rc;
-                    }
-                    BS_CUDA(cudaGraphLaunch(s->period_graph, s->stream));
-                    s->launches += s->period_kernels;
-                    s->list_valid = true;
-                    s->since_rebuild = K;
-                    remaining -= K;
-                    queued += K;
-                    continue;
-                }
-                s->launches += launch_rebuild(s->p, s->stream);
-                s->list_valid = true;
-                s->since_rebuild = 0;
-            }
-            const long long chunk = std::min<long long>(remaining, K - s->since_rebuild);
-            for (long long k = 0; k < chunk; ++k)
-                s->launches += launch_step(s->p, MODE_STEP, s->stream);
-            s->since_rebuild += static_cast<int>(chunk);
-            remaining -= chunk;
-            queued += chunk;
-        }
-        BS_CUDA(cudaGetLastError());
-        rc = read_ctl(s);
+        int rc = read_ctl(s);
         if (rc)
             return rc;
         const Ctl &h = *s->ctl_host;
@@ -723,17 +743,90 @@ int bs_step(bs_sim *s, int32_t nsteps)
             return fail(s, BS_E_NONFINITE, "Found non-finite position (a particle position became NaN or infinite)");
         if (h.status & (ST_CELL_CAPACITY | ST_PAIR_CAPACITY))
         {
-            rc = rebuild_now(s); // grows and rebuilds
+            rc = rebuild_now(s); // grows the lists and rebuilds
             if (rc)
                 return rc;
-            continue;
         }
-        if (h.status & ST_STALE)
+        else if (h.status & ST_STALE)
             s->list_valid = false; // the next rebuild clears the bit
+        if (s->steps_done >= s->target)
+            return BS_OK;
+        rc = enqueue_steps(s, s->target - s->steps_done);
+        if (rc)
+            return rc;
     }
-    if (s->steps_done < target)
-        return fail(s, BS_E_STATE, "bs_step: could not complete the requested steps");
+    return fail(s, BS_E_STATE, "bs_synchronize: could not complete the requested steps");
+}
+
+int bs_step(bs_sim *s, int32_t nsteps)
+{
+    const int rc = bs_step_async(s, nsteps);
+    return rc ? rc : bs_synchronize(s);
+}
+
+int bs_get_step_count(bs_sim *s, int64_t *steps)
+{
+    if (!s || !steps)
+        return fail(s, BS_E_ARG, "bs_get_step_count: null argument");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    const int rc = read_ctl(s);
+    if (rc)
+        return rc;
+    *steps = s->ctl_host->steps;
     return BS_OK;
+}
+
+int bs_get_stream(bs_sim *s, void **stream)
+{
+    if (!s || !stream)
+        return fail(s, BS_E_ARG, "bs_get_stream: null argument");
+    *stream = static_cast<void *>(s->stream);
+    return BS_OK;
+}
+
+int bs_launch_phase(bs_sim *s, int32_t phase)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    if (phase == 0)
+    {
+        s->launches += launch_rebuild(s->p, s->stream);
+        s->list_valid = true;
+        s->since_rebuild = 0;
+    }
+    else if (phase == 1)
+    {
+        s->launches += launch_step(s->p, MODE_STEP, s->stream);
+        s->target += 1;
+        s->since_rebuild += 1;
+    }
+    else
+        return fail(s, BS_E_ARG, "bs_launch_phase: phase must be 0 or 1");
+    BS_CUDA(cudaGetLastError());
+    return BS_OK;
+}
+
+int bs_set_external_forces(bs_sim *s, const float *f)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    if (!f)
+        return fail(s, BS_E_ARG, "bs_set_external_forces: null forces");
+    for (int64_t i = 0; i < s->n; ++i)
+        s->ext_host[i] = make_float4(f[3 * i], f[3 * i + 1], f[3 * i + 2], 0.f);
+    s->ext_dirty = true;
+    return BS_OK;
+}
+
+// Completes steps enqueued with bs_step_async before the state is read or replaced.
+static int settle(bs_sim *s)
+{
+    return s->target > s->steps_done ? bs_synchronize(s) : BS_OK;
 }
 
 int bs_compute_forces(bs_sim *s)
@@ -742,7 +835,10 @@ int bs_compute_forces(bs_sim *s)
         return fail(nullptr, BS_E_ARG, "null handle");
     if (!s->ready)
         return fail(s, BS_E_STATE, "bs_compute_forces: call bs_setup first");
-    int rc = sync_ext(s);
+    int rc = settle(s);
+    if (rc)
+        return rc;
+    rc = sync_ext(s);
     if (rc)
         return rc;
     if (!s->list_valid || (s->ctl_host->status & ST_STALE))
@@ -769,6 +865,9 @@ static int get_vec(bs_sim *s, int what, float *out)
         return fail(s, BS_E_STATE, "call bs_setup first");
     if (!out)
         return fail(s, BS_E_ARG, "null output");
+    const int rc = settle(s);
+    if (rc)
+        return rc;
     s->launches += launch_unsort(s->p, what, s->staging, s->stream);
     BS_CUDA(cudaGetLastError());
     BS_CUDA(cudaMemcpyAsync(out, s->staging, sizeof(float) * 3 * s->n, cudaMemcpyDeviceToHost, s->stream));
@@ -789,6 +888,9 @@ static int set_state(bs_sim *s, const float *xyz, const float *vel)
     const float *src = xyz ? xyz : vel;
     if (!src)
         return fail(s, BS_E_ARG, "null input");
+    const int rc = settle(s);
+    if (rc)
+        return rc;
     BS_CUDA(cudaMemcpyAsync(s->staging, src, sizeof(float) * 3 * s->n, cudaMemcpyHostToDevice, s->stream));
     s->launches += launch_set_positions(s->p, xyz ? s->staging : nullptr, xyz ? nullptr : s->staging, s->stream);
     BS_CUDA(cudaGetLastError());
@@ -822,6 +924,9 @@ int bs_get_energies(bs_sim *s, double out[BS_NUM_ENERGIES])
         return fail(nullptr, BS_E_ARG, "null handle");
     if (!s->ready)
         return fail(s, BS_E_STATE, "call bs_setup first");
+    const int rc = settle(s);
+    if (rc)
+        return rc;
     BS_CUDA(cudaMemcpyAsync(s->ctl_host->energies, s->p.ctl->energies, sizeof(double) * BS_NUM_ENERGIES,
                             cudaMemcpyDeviceToHost, s->stream));
     BS_CUDA(cudaStreamSynchronize(s->stream));
@@ -838,6 +943,11 @@ int bs_get_pairs(bs_sim *s, int32_t term, int64_t *out, int64_t cap, int64_t *n_
         return fail(s, BS_E_STATE, "call bs_setup first");
     if (term < BS_TERM_STERIC || term > BS_TERM_HYDROPHOBIC || cap < 0 || !n_out || (cap > 0 && !out))
         return fail(s, BS_E_ARG, "bs_get_pairs: bad arguments");
+    {
+        const int rc = settle(s);
+        if (rc)
+            return rc;
+    }
     if (!s->list_valid || (s->ctl_host->status & ST_STALE))
     {
         const int rc = rebuild_now(s);
@@ -887,6 +997,11 @@ int bs_get_cells(bs_sim *s, int32_t term, int64_t *out)
         return fail(s, BS_E_STATE, "call bs_setup first");
     if (term < BS_TERM_STERIC || term > BS_TERM_HYDROPHOBIC || !out)
         return fail(s, BS_E_ARG, "bs_get_cells: bad arguments");
+    {
+        const int rc = settle(s);
+        if (rc)
+            return rc;
+    }
     const bs_config &c = s->cfg;
     float cutoff = static_cast<float>(c.steric_cutoff);
     uint32_t need = 0;

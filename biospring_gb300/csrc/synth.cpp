@@ -56,7 +56,7 @@ struct Buckets
     bool any_within(const double * p, double r, const std::vector<double> & pts, int64_t skip) const
     {
         const int64_t cx = coord(p[0]), cy = coord(p[1]), cz = coord(p[2]);
-        const int64_t reach = static_cast<int64_t>(r / cell) + 1;
+        const int64_t reach = static_cast<int64_t>(std::ceil(r / cell));
         const double r2 = r * r;
         for (int64_t z = cz - reach; z <= cz + reach; ++z)
             for (int64_t y = cy - reach; y <= cy + reach; ++y)

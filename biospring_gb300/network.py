@@ -102,6 +102,27 @@ class SpringNetwork:
     def computeStep(self, nsteps: int = 1):
         self._check(self._lib.bs_step(self._h, int(nsteps)), self._h)
 
+    def computeStepAsync(self, nsteps: int = 1):
+        """Enqueues steps without waiting; :meth:`synchronize` completes them."""
+        self._check(self._lib.bs_step_async(self._h, int(nsteps)), self._h)
+
+    def synchronize(self):
+        self._check(self._lib.bs_synchronize(self._h), self._h)
+
+    def stepCount(self) -> int:
+        c = C.c_int64()
+        self._check(self._lib.bs_get_step_count(self._h, C.byref(c)), self._h)
+        return c.value
+
+    def stream(self) -> int:
+        """The cudaStream_t of the handle, as an integer."""
+        p = C.c_void_p()
+        self._check(self._lib.bs_get_stream(self._h, C.byref(p)), self._h)
+        return p.value or 0
+
+    def launchPhase(self, phase: int):
+        self._check(self._lib.bs_launch_phase(self._h, int(phase)), self._h)
+
     def computeForces(self):
         self._check(self._lib.bs_compute_forces(self._h), self._h)
 
@@ -131,6 +152,10 @@ class SpringNetwork:
     def setForce(self, i: int, f):
         f = _f32(f)
         self._check(self._lib.bs_set_force(self._h, int(i), ptr(f, C.c_float)), self._h)
+
+    def setExternalForces(self, f):
+        f = _f32(f, (-1, 3))
+        self._check(self._lib.bs_set_external_forces(self._h, ptr(f, C.c_float)), self._h)
 
     def energies(self) -> dict:
         out = np.zeros(6, dtype=np.float64)

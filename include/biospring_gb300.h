@@ -159,6 +159,26 @@ int bs_setup(bs_sim *sim, const bs_config *cfg);
  * bs_get_energies. Returns BS_E_NONFINITE if a position became non-finite. */
 int bs_step(bs_sim *sim, int32_t nsteps);
 
+/* Enqueues nsteps steps on the handle's stream and returns without waiting (the steps run as
+ * captured CUDA graphs). Status is checked by the next synchronising call. */
+int bs_step_async(bs_sim *sim, int32_t nsteps);
+
+/* Waits for enqueued work, checks the device status word and, if a particle drifted too far
+ * for the pair list or a list overflowed, rebuilds and completes the remaining steps. Returns
+ * BS_E_NONFINITE if a position became non-finite (SpringNetwork.cpp:222-229). */
+int bs_synchronize(bs_sim *sim);
+
+/* Number of steps the device has completed since bs_setup (synchronises). */
+int bs_get_step_count(bs_sim *sim, int64_t *steps);
+
+/* The CUDA stream (cudaStream_t) the handle launches on, for callers that order their own
+ * work or record CUDA events around the step. */
+int bs_get_stream(bs_sim *sim, void **stream);
+
+/* Enqueues one phase without waiting, for profiling: phase 0 = pair-list rebuild (cell list,
+ * counting sort, reorder, spring and pair lists), phase 1 = one step kernel. */
+int bs_launch_phase(bs_sim *sim, int32_t phase);
+
 /* Computes forces and energies at the current positions without integrating
  * (replaces idleRun() + computeForces(), SpringNetwork.cpp:244-249, 344-365).
  * The forces are then readable with bs_get_forces. */
@@ -176,6 +196,10 @@ int bs_set_velocities(bs_sim *sim, const float *vel);
 /* Adds an external force to particle i for the next step only (replaces
  * SpringNetwork::setForce, SpringNetwork.cpp:438-442, the interactor path). */
 int bs_set_force(bs_sim *sim, int64_t i, const float f[3]);
+
+/* Sets the external force of every particle for the next step (float[3n], caller order);
+ * the bulk form of bs_set_force used by interactive drivers every step. */
+int bs_set_external_forces(bs_sim *sim, const float *f);
 
 /* Energies of the last step or force evaluation, BS_ENERGY_* order, in kJ/mol
  * (SpringNetwork::getKineticEnergy ... getHydrophobicEnergy, SpringNetwork.h:157-162).

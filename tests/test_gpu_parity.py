@@ -1,0 +1,258 @@
+"""Parity of the CUDA path (through the C ABI) with the reference and the oracle.
+
+Bars (written in each test):
+  * pair sets and cell ids: bit-exact;
+  * forces: ||F_gpu - F_ref||_2 / ||F_ref||_2 <= 1e-5 over the dynamic particles, and no
+    worse than 4x the reference arithmetic's own distance to FP64 when that is larger;
+  * energies: relative 1e-5 (or the reference's own FP32 error vs FP64, whichever is larger);
+  * trajectories: positions within 1e-4 A after tens of damped steps.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+from helpers import dynamic_mask, gpu_network, load_golden, rel_l2, rel_scalar, system_from_golden
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+
+FORCE_TOL = 1e-5
+ENERGY_TOL = 1e-5
+
+
+def force_tolerance(system, f_ref):
+    """1e-5, or 4x the FP32 reference's own relative distance to FP64 if that is larger."""
+    orc = po.Oracle(system)
+    f64, _ = orc.eval_fp64()
+    own = rel_l2(f_ref, f64, dynamic_mask(system))
+    orc.close()
+    return max(FORCE_TOL, 4.0 * own), own
+
+
+def energy_ok(e_gpu, e_ref, e64, k):
+    own = abs(e_ref[k] - e64[k])
+    return abs(e_gpu[k] - e_ref[k]) <= max(ENERGY_TOL * abs(e_ref[k]), 4.0 * own) + 1e-9
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2, 3])
+def test_mixed_forces_energies_pairs_cells(mode):
+    """All nonbonded terms, static particles, IMPALA, viscosity; every steric mode."""
+    g = load_golden(f"mixed_m{mode}.npz")
+    s = system_from_golden(g)
+    net = gpu_network(s)
+    net.computeForces()
+    f = net.getForces()
+    dyn = dynamic_mask(s)
+    tol, own = force_tolerance(s, g["force0"])
+    err = rel_l2(f, g["force0"], dyn)
+    print(f"mode {mode}: force rel err {err:.3e} (reference vs FP64 {own:.3e})")
+    assert err <= tol
+    e = np.array(list(net.energies().values()))
+    orc = po.Oracle(s)
+    _, e64 = orc.eval_fp64()
+    for k in (2, 3, 4, 5):
+        assert energy_ok(e, g["energy0"], e64, k), (k, e[k], g["energy0"][k], e64[k])
+    if mode == 1:
+        for term in (0, 1, 2):
+            np.testing.assert_array_equal(net.getPairs(term), g[f"pairs{term}"].astype(np.int64))
+            np.testing.assert_array_equal(net.getCells(term), g[f"cells{term}"].astype(np.int64))
+    net.computeStep(3)
+    x = net.getPositions()
+    assert np.abs(x - g["pos3"]).max() < 1e-4
+    net.close()
+
+
+def test_regression_scans():
+    """Two-particle scans of the reference's regression tests (energies and forces)."""
+    from biospring_gb300 import workloads as W
+    g = load_golden("scans.npz")
+    xs = g["x"]
+    cc = dict(charge=np.full(2, 0.5973, np.float32), radius=np.full(2, 1.908, np.float32),
+              epsilon=np.full(2, 0.086, np.float32), mass=np.full(2, 12.01, np.float32))
+    base = dict(nbsteps=1, timestep=0.01)
+    cases = {
+        "spring": (dict(base, spring_enable=1), dict(ij=np.array([[0, 1]], np.int32), r0=np.zeros(1, np.float32),
+                                                     k=np.ones(1, np.float32)), cc, 1),
+        "steric_linear": (dict(base, steric_enable=1, steric_cutoff=16.0, steric_mode=0), {}, cc, 2),
+        "steric_amber": (dict(base, steric_enable=1, steric_cutoff=16.0, steric_mode=1), {}, cc, 2),
+        "coulomb": (dict(base, coulomb_enable=1, coulomb_cutoff=16.0, coulomb_dielectric=1.0), {}, cc, 3),
+        "hydrophobic": (dict(base, hydrophobicity_enable=1, hydrophobicity_cutoff=16.0), {},
+                        dict(hydrophobicity=np.array([0.5, 0.3], np.float32)), 5),
+    }
+    for name, (cfg, sp, props, slot) in cases.items():
+        s = W.System("two", np.zeros((2, 3), np.float32), sp.get("ij", np.zeros((0, 2), np.int32)),
+                     sp.get("r0", np.zeros(0, np.float32)), sp.get("k", np.zeros(0, np.float32)), cfg, **props)
+        net = gpu_network(s)
+        ref_e = g[f"{name}_energy"][:, slot]
+        ref_f = g[f"{name}_force"][:, 0, 0].astype(np.float64)
+        got_e = np.zeros_like(ref_e)
+        got_f = np.zeros_like(ref_f)
+        for t, x in enumerate(xs):
+            net.setPositions(np.array([[0, 0, 0], [x, 0, 0]], np.float32))
+            net.computeForces()
+            got_e[t] = list(net.energies().values())[slot]
+            got_f[t] = net.getForces()[0, 0]
+        # Energies: the reference's own tiered absolute tolerances (test-steric-energy.cpp:141-159),
+        # which are looser than 1e-5 relative only where the LJ energy exceeds 1e4 kJ/mol.
+        mag = np.abs(ref_e)
+        tol_e = np.where(mag < 1e4, np.maximum(1e-3 * (name == "steric_amber"), 1e-5 * mag),
+                         np.where(mag < 1e5, 1e-2, np.where(mag < 1e8, 1e1, 1e7)))
+        tol_e = np.maximum(tol_e, 1e-5 * mag)
+        bad_e = np.abs(got_e - ref_e) > tol_e + 1e-12
+        # Forces: 1e-5 relative to the local magnitude; at the LJ force zero crossing the
+        # scale is the scan's typical force there (1e-5 of the largest force within 0.5 A).
+        scale = np.array([np.abs(ref_f[max(0, t - 50):t + 50]).max() for t in range(len(ref_f))])
+        bad_f = np.abs(got_f - ref_f) > 1e-5 * np.maximum(np.abs(ref_f), 1e-2 * scale) + 1e-30
+        print(f"{name}: energy max rel {np.max(np.abs(got_e - ref_e) / np.maximum(mag, 1e-12)):.2e}, "
+              f"points out of tolerance: energy {int(bad_e.sum())}, force {int(bad_f.sum())}")
+        assert not bad_e.any() and not bad_f.any(), name
+        net.close()
+
+
+def test_ca_network_trajectory_matches_reference():
+    g = load_golden("ca300.npz")
+    s = system_from_golden(g)
+    net = gpu_network(s)
+    done = 0
+    for mark in (1, 10, 30):
+        net.computeStep(mark - done)
+        done = mark
+        x = net.getPositions()
+        v = net.getVelocities()
+        assert np.abs(x - g[f"pos_{mark}"]).max() < 1e-4
+        assert rel_l2(v, g[f"vel_{mark}"]) < 1e-4
+        e = np.array(list(net.energies().values()))
+        assert rel_scalar(e[1], g[f"energy_{mark}"][1]) < 1e-5
+        assert rel_scalar(e[0], g[f"energy_{mark}"][0]) < 1e-4
+
+
+def test_neighbour_search_pairs_and_cells():
+    g = load_golden("nsearch.npz")
+    s = system_from_golden(g)
+    net = gpu_network(s)
+    np.testing.assert_array_equal(net.getPairs(0), g["pairs0"].astype(np.int64))
+    np.testing.assert_array_equal(net.getCells(0), g["cells0"].astype(np.int64))
+
+
+def test_uniform_lj_against_oracle_and_fp64():
+    """20,000 particles at the density of the 100k system; constant dielectric (reference mode)."""
+    from biospring_gb300 import workloads as W
+    s = W.uniform_lj(n=20000, box=160.0 * (0.2 ** (1 / 3)), seed=7)
+    net = gpu_network(s)
+    orc = po.Oracle(s)
+    net.computeForces()
+    orc.compute_forces()
+    f_gpu, f_orc = net.getForces(), orc.forces()
+    f64, e64 = orc.eval_fp64()
+    err = rel_l2(f_gpu, f_orc)
+    own = rel_l2(f_orc, f64)
+    gerr = rel_l2(f_gpu, f64)
+    print(f"uniform LJ 20k: gpu vs reference-arithmetic {err:.3e}, gpu vs FP64 {gerr:.3e}, "
+          f"reference-arithmetic vs FP64 {own:.3e}")
+    assert err <= max(FORCE_TOL, 4 * own)
+    for term in (0, 1):
+        np.testing.assert_array_equal(net.getPairs(term), orc.pairs(term))
+        np.testing.assert_array_equal(net.getCells(term), orc.cells(term))
+    e_gpu = np.array(list(net.energies().values()))
+    e_orc = orc.energies()
+    for k in (1, 2, 3):
+        assert energy_ok(e_gpu, e_orc, e64, k), (k, e_gpu[k], e_orc[k], e64[k])
+
+
+def test_distance_dielectric_against_fp64():
+    """eps = 4 r (no reference counterpart): checked against the FP64 restatement."""
+    from biospring_gb300 import workloads as W
+    s = W.uniform_lj(n=20000, box=160.0 * (0.2 ** (1 / 3)), seed=8, dielectric_mode=1)
+    net = gpu_network(s)
+    orc = po.Oracle(s)
+    net.computeForces()
+    orc.compute_forces()
+    f64, e64 = orc.eval_fp64()
+    gerr = rel_l2(net.getForces(), f64)
+    own = rel_l2(orc.forces(), f64)
+    print(f"eps=4r: gpu vs FP64 {gerr:.3e}, FP32 restatement vs FP64 {own:.3e}")
+    assert gerr <= max(FORCE_TOL, 4 * own)
+    e = np.array(list(net.energies().values()))
+    assert rel_scalar(e[3], e64[3]) < 1e-5
+
+
+def test_long_trajectory_tracks_oracle():
+    """2,000-particle Calpha network, 200 damped steps (the plain CPU/GPU configuration)."""
+    from biospring_gb300 import workloads as W
+    s = W.ca_network(n=2000, seed=1)
+    net = gpu_network(s)
+    orc = po.Oracle(s)
+    net.computeStep(200)
+    orc.step(200)
+    dx = np.abs(net.getPositions() - orc.positions()).max()
+    e_gpu = np.array(list(net.energies().values()))
+    e_orc = orc.energies()
+    print(f"ca2000 after 200 steps: max |dx| {dx:.3e} A, spring energy {e_gpu[1]:.6f} vs {e_orc[1]:.6f}")
+    assert dx < 1e-3
+    assert rel_scalar(e_gpu[1], e_orc[1]) < 1e-4
+
+
+def test_deterministic_bitwise():
+    from biospring_gb300 import workloads as W
+    s = W.uniform_lj(n=5000, box=160.0 * (0.05 ** (1 / 3)), seed=9)
+    out = []
+    for _ in range(2):
+        net = gpu_network(s)
+        net.computeStep(25)
+        out.append((net.getPositions(), net.getVelocities(), net.energies()))
+        net.close()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+
+
+def test_nonfinite_position_is_reported():
+    """SpringNetwork.cpp:222-229 dies on a non-finite position; the C ABI returns BS_E_NONFINITE."""
+    from biospring_gb300 import BsError, capi, workloads as W
+    s = W.ca_network(n=300, seed=2)
+    net = gpu_network(s)
+    x = net.getPositions()
+    x[17, 0] = np.nan  # planted on the host
+    net.setPositions(x)
+    with pytest.raises(BsError) as ei:
+        net.computeStep(2)
+    assert ei.value.code == capi.BS_E_NONFINITE
+
+
+def test_external_force_applies_for_one_step():
+    """SpringNetwork::setForce adds a force consumed by the next step (SpringNetwork.cpp:438-442)."""
+    from biospring_gb300 import workloads as W
+    s = W.ca_network(n=300, seed=3)
+    a = gpu_network(s)
+    b = gpu_network(s)
+    b.setForce(5, [0.5, 0.0, 0.0])
+    a.computeStep(1)
+    b.computeStep(1)
+    va, vb = a.getVelocities(), b.getVelocities()
+    dt = s.config["timestep"]
+    assert abs((vb[5, 0] - va[5, 0]) - 0.5 * dt) < 1e-6
+    a.computeStep(1)
+    b.computeStep(1)
+    # no force on the second step: the velocity difference decays only through viscosity
+    dv = b.getVelocities()[5, 0] - a.getVelocities()[5, 0]
+    assert dv < 0.5 * dt
+
+
+def test_errors_match_reference_exceptions():
+    from biospring_gb300 import BsError, SpringNetwork, capi
+    net = SpringNetwork()
+    net.addParticles(np.zeros((3, 3), np.float32))
+    with pytest.raises(BsError) as ei:
+        net.addSprings([[0, 3]], [1.0], [1.0])
+    assert ei.value.code == capi.BS_E_ARG
+    with pytest.raises(BsError):
+        net.addSprings([[1, 1]], [1.0], [1.0])
+    with pytest.raises(BsError) as ei:
+        net.setup(dict(steric_enable=1, steric_cutoff=0.0))
+    assert "Steric cutoff" in str(ei.value)
+    with pytest.raises(BsError) as ei:
+        net.computeStep(1)
+    assert ei.value.code == capi.BS_E_STATE

@@ -74,6 +74,9 @@ struct bs_sim
     cudaGraphExec_t period_graph = nullptr;
     int period_kernels = 0;
     long long launches = 0;
+    // growable buffers (pair lists, grid arrays), freed on regrowth
+    unsigned int *pl_idx[kTerms] = {nullptr, nullptr, nullptr};
+    int *cell_buf[3] = {nullptr, nullptr, nullptr};
     // diagnostics scratch
     long long *diag_out = nullptr;
     unsigned long long *diag_count = nullptr;
@@ -113,9 +116,14 @@ void destroy_graph(bs_sim *s)
     }
 }
 
+void free_growable(bs_sim *s);
+
 void release_device(bs_sim *s)
 {
     destroy_graph(s);
+    if (s->stream)
+        cudaStreamSynchronize(s->stream);
+    free_growable(s);
     s->dev.free_all();
     s->diag_out = nullptr;
     s->diag_count = nullptr;
@@ -152,27 +160,54 @@ int clear_status(bs_sim *s, int bits)
     return BS_OK;
 }
 
-// (Re)allocates the pair list and the cell arrays for the given capacities.
-int alloc_lists(bs_sim *s, int pl_cap, int cell_cap)
+// Frees the growable buffers (pair lists and grid arrays).
+void free_growable(bs_sim *s)
+{
+    for (int t = 0; t < kTerms; ++t)
+    {
+        if (s->pl_idx[t])
+            cudaFree(s->pl_idx[t]);
+        s->pl_idx[t] = nullptr;
+    }
+    for (int k = 0; k < 3; ++k)
+    {
+        if (s->cell_buf[k])
+            cudaFree(s->cell_buf[k]);
+        s->cell_buf[k] = nullptr;
+    }
+}
+
+// (Re)allocates the three pair lists and the cell arrays for the given capacities. The stream
+// is idle when this runs (callers synchronise first), so the old buffers can be released.
+int alloc_lists(bs_sim *s, const int caps[kTerms], int cell_cap)
 {
     Params &p = s->p;
-    // Pair list and grid arrays are the only buffers that grow; they are allocated apart.
-    static_assert(sizeof(int) == 4, "int32 expected");
-    int *pl = nullptr, *cs = nullptr, *cc = nullptr, *cf = nullptr;
-    BS_CUDA(s->dev.alloc(&pl, static_cast<size_t>(p.npad) * pl_cap));
-    BS_CUDA(s->dev.alloc(&cc, static_cast<size_t>(cell_cap) + 1));
-    BS_CUDA(s->dev.alloc(&cs, static_cast<size_t>(cell_cap) + 1));
-    BS_CUDA(s->dev.alloc(&cf, static_cast<size_t>(cell_cap) + 1));
-    BS_CUDA(cudaMemsetAsync(cc, 0, (static_cast<size_t>(cell_cap) + 1) * sizeof(int), s->stream));
-    // Old arrays are kept alive by the handle until destroy (growth is rare).
-    p.pl = pl;
-    p.pl_cap = pl_cap;
-    p.cell_cnt = cc;
-    p.cell_start = cs;
-    p.cell_fill = cf;
+    BS_CUDA(cudaStreamSynchronize(s->stream));
+    free_growable(s);
+    for (int t = 0; t < kTerms; ++t)
+    {
+        const int cap = p.pl[t].on ? std::max(caps[t], 1) : 1;
+        BS_CUDA(cudaMalloc(reinterpret_cast<void **>(&s->pl_idx[t]),
+                           static_cast<size_t>(p.npad) * cap * sizeof(unsigned int)));
+        p.pl[t].idx = s->pl_idx[t];
+        p.pl[t].cap = cap;
+    }
+    for (int k = 0; k < 3; ++k)
+        BS_CUDA(cudaMalloc(reinterpret_cast<void **>(&s->cell_buf[k]), (static_cast<size_t>(cell_cap) + 1) * sizeof(int)));
+    BS_CUDA(cudaMemsetAsync(s->cell_buf[0], 0, (static_cast<size_t>(cell_cap) + 1) * sizeof(int), s->stream));
+    p.cell_cnt = s->cell_buf[0];
+    p.cell_start = s->cell_buf[1];
+    p.cell_fill = s->cell_buf[2];
     p.cell_cap = cell_cap;
     destroy_graph(s);
     return BS_OK;
+}
+
+int current_caps(const bs_sim *s, int caps[kTerms])
+{
+    for (int t = 0; t < kTerms; ++t)
+        caps[t] = s->p.pl[t].cap;
+    return 0;
 }
 
 int sync_ext(bs_sim *s)
@@ -210,7 +245,9 @@ int rebuild_now(bs_sim *s)
             const long long need = s->ctl_host->ncells_needed;
             if (need > (1ll << 28))
                 return fail(s, BS_E_CAPACITY, "search grid needs more than 2^28 cells (particles spread too far)");
-            rc = alloc_lists(s, s->p.pl_cap, static_cast<int>(need + need / 2 + 64));
+            int caps[kTerms];
+            current_caps(s, caps);
+            rc = alloc_lists(s, caps, static_cast<int>(need + need / 2 + 64));
             if (rc)
                 return rc;
             rc = clear_status(s, ST_CELL_CAPACITY);
@@ -220,10 +257,17 @@ int rebuild_now(bs_sim *s)
         }
         if (st & ST_PAIR_CAPACITY)
         {
-            const int need = s->ctl_host->max_row;
-            if (static_cast<double>(need) * s->p.npad > 2.0e9)
-                return fail(s, BS_E_CAPACITY, "pair list would exceed 2^31 entries");
-            rc = alloc_lists(s, need + need / 4 + 16, s->p.cell_cap);
+            int caps[kTerms];
+            current_caps(s, caps);
+            for (int t = 0; t < kTerms; ++t)
+            {
+                const int need = s->ctl_host->max_row[t];
+                if (need > caps[t])
+                    caps[t] = need + need / 8 + 8;
+                if (static_cast<double>(caps[t]) * s->p.npad > 2.0e9)
+                    return fail(s, BS_E_CAPACITY, "pair list would exceed 2^31 entries");
+            }
+            rc = alloc_lists(s, caps, s->p.cell_cap);
             if (rc)
                 return rc;
             rc = clear_status(s, ST_PAIR_CAPACITY);
@@ -468,16 +512,16 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     for (int64_t i = 0; i < n; ++i)
         row[i + 1] = row[i] + deg[i];
     const int nnz = row[n];
-    std::vector<int> col(std::max(nnz, 1));
+    std::vector<unsigned int> col(std::max(nnz, 1));
     std::vector<float> kk(std::max(nnz, 1)), rr(std::max(nnz, 1));
     std::vector<int> fillp(row.begin(), row.end() - 1);
     auto partner_code = [&](int a, int b) {
         uint32_t code = static_cast<uint32_t>(b);
         if (s->is_static[b])
-            code |= 0x80000000u;
+            code |= kEntryStatic;
         if (s->rigid[a] && s->rigid[b])
-            code |= 0x40000000u;
-        return static_cast<int>(code);
+            code |= kEntryInactive;
+        return code;
     };
     for (size_t t = 0; t < s->sp_i.size(); ++t)
     {
@@ -497,20 +541,32 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     p.sp_maxdeg = maxdeg;
 
     // ---- per-particle packed parameters ----
-    std::vector<float4> pos0(npad), vel0(npad), jprm0(npad), iprm0(npad);
+    // Steric factors: eps_ij r_ij^m = (a_i b_i^m)(a_j b_j^m) with eps_ij = a_i a_j, r_ij = b_i b_j
+    // (CombinationRules.hpp:18-31); P = a b^6 rides in pos.w, fhi = a b^12 (Amber) or a b^8.
+    std::vector<float4> pos0(npad), vel0(npad), iprm0(npad);
+    std::vector<float> fhi0(npad, 0.f), chg0(npad, 0.f), hyd0(npad, 0.f);
+    std::vector<unsigned int> flags0(npad, PF_STATIC);
     for (int64_t i = 0; i < n; ++i)
     {
-        pos0[i] = make_float4(s->xyz[3 * i], s->xyz[3 * i + 1], s->xyz[3 * i + 2], s->charge[i]);
-        vel0[i] = make_float4(s->vel[3 * i], s->vel[3 * i + 1], s->vel[3 * i + 2], 0.f);
-        float a = 0.f, b = s->radius[i];
+        double P = s->radius[i], F = 0.0;
+        const double eps = s->eps[i], rad = s->radius[i];
         if (c.steric_mode == BS_STERIC_LJ_12_6_AMBER || c.steric_mode == BS_STERIC_LJ_8_6_LEWITT)
         {
-            a = std::sqrt(s->eps[i]);
-            b = std::sqrt(s->radius[i]);
+            // a = sqrt(eps), b = sqrt(r): P = a b^6 = sqrt(eps) r^3, fhi = a b^12 or a b^8
+            P = std::sqrt(eps) * rad * rad * rad;
+            F = std::sqrt(eps) * std::pow(rad, c.steric_mode == BS_STERIC_LJ_12_6_AMBER ? 6 : 4);
         }
         else if (c.steric_mode == BS_STERIC_LJ_8_6_ZACHARIAS)
-            a = s->eps[i];
-        uint32_t flags = 0;
+        {
+            P = eps * std::pow(rad, 6);
+            F = eps * std::pow(rad, 8);
+        }
+        pos0[i] = make_float4(s->xyz[3 * i], s->xyz[3 * i + 1], s->xyz[3 * i + 2], static_cast<float>(P));
+        vel0[i] = make_float4(s->vel[3 * i], s->vel[3 * i + 1], s->vel[3 * i + 2], 0.f);
+        fhi0[i] = static_cast<float>(F);
+        chg0[i] = s->charge[i];
+        hyd0[i] = s->hydro[i];
+        unsigned int flags = 0;
         if (s->is_static[i])
             flags |= PF_STATIC;
         if (s->charge[i] != 0.0f)
@@ -519,9 +575,7 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
             flags |= PF_HYDROPHOBIC;
         if (s->rigid[i])
             flags |= PF_RIGID;
-        float fw;
-        std::memcpy(&fw, &flags, sizeof(fw));
-        jprm0[i] = make_float4(a, b, s->hydro[i], fw);
+        flags0[i] = flags;
         iprm0[i] = make_float4(s->mass[i], s->sasa[i], s->transfer[i], 0.f);
     }
     std::vector<int> perm0(npad, 0), inv0(n);
@@ -536,7 +590,10 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     {
         BS_CUDA(s->dev.alloc(&p.pos[b], npad));
         BS_CUDA(s->dev.alloc(&p.vel[b], npad));
-        BS_CUDA(s->dev.alloc(&p.jprm[b], npad));
+        BS_CUDA(s->dev.alloc(&p.fhi[b], npad));
+        BS_CUDA(s->dev.alloc(&p.chg[b], npad));
+        BS_CUDA(s->dev.alloc(&p.hyd[b], npad));
+        BS_CUDA(s->dev.alloc(&p.flags[b], npad));
         BS_CUDA(s->dev.alloc(&p.iprm[b], npad));
         BS_CUDA(s->dev.alloc(&p.perm[b], npad));
     }
@@ -544,7 +601,8 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     BS_CUDA(s->dev.alloc(&p.pos_build, npad));
     BS_CUDA(s->dev.alloc(&p.ext, n));
     BS_CUDA(s->dev.alloc(&p.force_out, n));
-    int *d_row, *d_col;
+    int *d_row;
+    unsigned int *d_col;
     float *d_k, *d_r0;
     BS_CUDA(s->dev.alloc(&d_row, n + 1));
     BS_CUDA(s->dev.alloc(&d_col, std::max(nnz, 1)));
@@ -558,7 +616,8 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     BS_CUDA(s->dev.alloc(&p.se_k, static_cast<size_t>(npad) * maxdeg));
     BS_CUDA(s->dev.alloc(&p.se_r0, static_cast<size_t>(npad) * maxdeg));
     BS_CUDA(s->dev.alloc(&p.se_deg, npad));
-    BS_CUDA(s->dev.alloc(&p.pl_cnt, npad));
+    for (int t = 0; t < kTerms; ++t)
+        BS_CUDA(s->dev.alloc(&p.pl[t].cnt, npad));
     BS_CUDA(s->dev.alloc(&p.cell_of, npad));
     BS_CUDA(s->dev.alloc(&p.tmp_perm, npad));
     s->step_blocks = (p.n + kStepBlock - 1) / kStepBlock;
@@ -569,12 +628,20 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     BS_CUDA(cudaMallocHost(reinterpret_cast<void **>(&s->ext_host), sizeof(float4) * n));
     std::memset(s->ext_host, 0, sizeof(float4) * n);
 
-    // initial grid capacity from the current bounding box
-    const double list_radius = static_cast<float>(std::max({c.steric_enable ? c.steric_cutoff : 0.0,
-                                                            c.coulomb_enable ? c.coulomb_cutoff : 0.0,
-                                                            c.hydrophobicity_enable ? c.hydrophobicity_cutoff : 0.0,
-                                                            1e-3}) +
-                                                   c.list_skin);
+    // ---- pair lists: which terms, radii, first capacities from the density ----
+    const double skin = c.list_skin;
+    const double cut[kTerms] = {c.steric_cutoff, c.coulomb_cutoff, c.hydrophobicity_cutoff};
+    const int on[kTerms] = {c.steric_enable != 0, c.coulomb_enable != 0, c.hydrophobicity_enable != 0};
+    double list_radius = 1e-3;
+    for (int t = 0; t < kTerms; ++t)
+    {
+        p.pl[t].on = on[t];
+        const double R = static_cast<float>(cut[t]) + skin;
+        p.pl[t].r2 = static_cast<float>(R * R * (1.0 + 1e-5));
+        if (on[t])
+            list_radius = std::max(list_radius, R);
+    }
+    p.list_radius = static_cast<float>(list_radius);
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (int64_t i = 0; i < n; ++i)
         for (int k = 0; k < 3; ++k)
@@ -582,19 +649,34 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
             lo[k] = std::min(lo[k], static_cast<double>(s->xyz[3 * i + k]));
             hi[k] = std::max(hi[k], static_cast<double>(s->xyz[3 * i + k]));
         }
-    double cells = 1.0;
+    double cells = 1.0, volume = 1.0;
     for (int k = 0; k < 3; ++k)
+    {
         cells *= std::ceil((hi[k] - lo[k]) / list_radius) + 3.0;
+        volume *= std::max(hi[k] - lo[k], 1.0);
+    }
     const int cell_cap = static_cast<int>(std::min(2.0 * cells + 1024.0, 2.0e8));
-    const int pl_cap = 64;
-    int rc = alloc_lists(s, pl_cap, cell_cap);
+    // first capacity: 1.5x the mean count expected in the list sphere, at least 32
+    int caps[kTerms];
+    const double density = static_cast<double>(n) / volume;
+    for (int t = 0; t < kTerms; ++t)
+    {
+        const double R = static_cast<float>(cut[t]) + skin;
+        const double expect = density * 4.18879 * R * R * R;
+        caps[t] = static_cast<int>(std::min(std::max(1.5 * expect + 16.0, 32.0), 4096.0));
+    }
+    int rc = alloc_lists(s, caps, cell_cap);
     if (rc)
         return rc;
 
     // ---- uploads ----
     BS_CUDA(cudaMemcpyAsync(p.pos[0], pos0.data(), sizeof(float4) * npad, cudaMemcpyHostToDevice, s->stream));
     BS_CUDA(cudaMemcpyAsync(p.vel[0], vel0.data(), sizeof(float4) * npad, cudaMemcpyHostToDevice, s->stream));
-    BS_CUDA(cudaMemcpyAsync(p.jprm[0], jprm0.data(), sizeof(float4) * npad, cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(p.fhi[0], fhi0.data(), sizeof(float) * npad, cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(p.chg[0], chg0.data(), sizeof(float) * npad, cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(p.hyd[0], hyd0.data(), sizeof(float) * npad, cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(p.flags[0], flags0.data(), sizeof(unsigned int) * npad, cudaMemcpyHostToDevice,
+                            s->stream));
     BS_CUDA(cudaMemcpyAsync(p.iprm[0], iprm0.data(), sizeof(float4) * npad, cudaMemcpyHostToDevice, s->stream));
     BS_CUDA(cudaMemcpyAsync(p.perm[0], perm0.data(), sizeof(int) * npad, cudaMemcpyHostToDevice, s->stream));
     BS_CUDA(cudaMemcpyAsync(p.inv, inv0.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
@@ -631,16 +713,6 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     p.hi2_c = band_hi2(p.c_coulomb);
     p.lo2_h = band_lo2(p.c_hydro);
     p.hi2_h = band_hi2(p.c_hydro);
-    float r2_any = 0.f;
-    if (p.steric_on)
-        r2_any = std::max(r2_any, p.hi2_s);
-    if (p.coulomb_on)
-        r2_any = std::max(r2_any, p.hi2_c);
-    if (p.hydro_on)
-        r2_any = std::max(r2_any, p.hi2_h);
-    p.r2_any = r2_any;
-    p.list_radius = static_cast<float>(list_radius);
-    p.list_r2 = static_cast<float>(list_radius * list_radius * (1.0 + 1e-5));
     const double hs = 0.5 * c.list_skin * (1.0 - 1e-5);
     p.half_skin2 = static_cast<float>(hs * hs);
     p.spring_scale = static_cast<float>(c.spring_scale);
@@ -648,13 +720,14 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     p.coulomb_scale = static_cast<float>(c.coulomb_scale);
     p.hydro_scale = static_cast<float>(c.hydrophobicity_scale);
     p.imp_scale = static_cast<float>(c.impala_scale);
-    p.dielectric = static_cast<float>(c.coulomb_dielectric);
     p.visc = static_cast<float>(c.viscosity_value);
     p.imp_z0 = static_cast<float>(c.impala_z0);
     p.imp_alpha = static_cast<float>(c.impala_alpha);
+    const double D = static_cast<float>(c.coulomb_dielectric);
+    const double cs = static_cast<float>(c.coulomb_scale);
     p.k_spring_f = static_cast<float>(kSpringForceConvert);
-    p.k_elec_e = static_cast<float>(kCoulombEnergyPerA);
-    p.k_elec_f = static_cast<float>(kElecForceConvert / (4.0 * kPi));
+    p.k_elec_e = static_cast<float>(kCoulombEnergyPerA * cs / D);
+    p.k_elec_f = static_cast<float>(kElecForceConvert / (4.0 * kPi) * cs / D);
     p.k_kin = static_cast<float>(kKineticConvert);
     p.k_imp_f = static_cast<float>(kImpForceConvert);
     p.k_hydro_e = static_cast<float>(kAvogadro * 1.0E-3);

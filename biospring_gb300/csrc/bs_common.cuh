@@ -41,7 +41,7 @@ enum : int
     ST_STALE = 8,           // a particle drifted more than half the list skin: rebuild needed
 };
 
-// particle flag bits (stored as the integer bits of jprm.w)
+// particle flag bits
 enum : uint32_t
 {
     PF_STATIC = 1u,
@@ -49,6 +49,13 @@ enum : uint32_t
     PF_HYDROPHOBIC = 4u,
     PF_RIGID = 8u,
 };
+
+// list entry bits: the low 30 bits are a slot
+constexpr uint32_t kSlotMask = 0x3fffffffu;
+constexpr uint32_t kEntryStatic = 0x80000000u;   // the partner is static: the pair's full energy is ours
+constexpr uint32_t kEntryInactive = 0x40000000u; // spring between two rigid particles: no force
+
+constexpr int kTerms = 3; // steric, Coulomb, hydrophobic pair lists
 
 // Device control block: one per simulation handle, in device memory.
 struct Ctl
@@ -60,7 +67,7 @@ struct Ctl
     unsigned int done_bbox;
     unsigned int done_reorder;
     long long steps;          // completed steps since setup
-    int max_row;              // largest pair-list row seen at the last build
+    int max_row[kTerms];      // largest pair-list row of each term seen at the last build
     int ncells_needed;
     // search grid of the current layout (reference formula, nsearch.hpp:342-354)
     double gmin[3];
@@ -69,7 +76,17 @@ struct Ctl
     unsigned int bbox_enc[6];  // order-preserving codes of min xyz, max xyz (reset after use)
     int status_pending;        // bits raised during a step, merged into status by its last block
     int ext_pending;           // an external force waits in Params::ext
-    double energies[8];       // BS_ENERGY_* of the last evaluation
+    double energies[8];        // BS_ENERGY_* of the last evaluation
+};
+
+// One typed pair list: ELL, column-major [k * npad + slot], entries = slot | kEntryStatic.
+struct PairList
+{
+    unsigned int *idx;
+    int *cnt;                 // [npad]
+    int cap;
+    float r2;                 // squared list radius (cutoff + skin), slightly inflated
+    int on;
 };
 
 // Step parameters passed by value to the kernels.
@@ -77,59 +94,58 @@ struct Params
 {
     int n;                    // particles
     int npad;                 // n rounded up to a multiple of 32 (ELL row stride)
-    // double-buffered sorted state, indexed by Ctl::sbuf / Ctl::lbuf
-    float4 *pos[2];           // x, y, z, charge
+    // double-buffered sorted state: positions/velocities flip every step (Ctl::sbuf), the
+    // per-particle parameters flip at every rebuild (Ctl::lbuf)
+    float4 *pos[2];           // x, y, z, steric factor P (F6 for LJ modes, radius for linear)
     float4 *vel[2];           // vx, vy, vz, 0
-    float4 *jprm[2];          // steric a, steric b, hydrophobicity, flags (as bits)
+    float *fhi[2];            // second steric factor (F12 Amber, F8 Lewitt/Zacharias)
+    float *chg[2];            // charge
+    float *hyd[2];            // hydrophobicity
+    unsigned int *flags[2];   // PF_* bits
+    float4 *iprm[2];          // mass, sasa, transfer, 0
     int *perm[2];             // sorted slot -> caller id
     int *inv;                 // caller id -> sorted slot (current layout)
     float4 *pos_build;        // positions at the last pair-list build (sorted)
-    float4 *iprm[2];          // mass, sasa, transfer, 0 (sorted, re-laid out with jprm)
     // per-particle data in caller order
-    float4 *ext;              // external force for the next step (caller order)
-    float4 *force_out;        // forces of a force-only evaluation (caller order)
-    // springs: caller-order CSR (static topology)
+    float4 *ext;              // external force for the next step
+    float4 *force_out;        // forces of a force-only evaluation
+    // springs: caller-order CSR (static topology), partner | kEntryStatic | kEntryInactive
     const int *sp_row;        // [n+1]
-    const int *sp_col;        // partner caller id, bit 31 = partner is static
+    const unsigned int *sp_col;
     const float *sp_k;
     const float *sp_r0;
     int sp_maxdeg;
-    // springs: sorted-space ELL, column-major [k * npad + slot]
-    int *se_col;              // partner slot, bit 31 = partner static; -1 = none
+    // springs: sorted-space ELL, column-major [k * npad + slot], each row ascending by partner slot
+    unsigned int *se_col;
     float *se_k;
     float *se_r0;
     int *se_deg;              // [npad]
-    // pair list: ELL column-major [k * npad + slot]
-    int *pl;
-    int *pl_cnt;              // [npad]
-    int pl_cap;
+    // nonbonded pair lists
+    PairList pl[kTerms];
     // search grid
-    int *cell_of;             // [n] cell of each sorted slot (new layout)
+    int *cell_of;             // [npad] cell of each sorted slot (new layout)
     int *cell_cnt;            // [cell_cap + 1]
     int *cell_start;          // [cell_cap + 1]
     int *cell_fill;           // [cell_cap]
-    int *tmp_perm;            // [n]
+    int *tmp_perm;            // [npad]
     int cell_cap;
     // energies: per-block partials
-    double *blk_energy;       // [max_blocks * 8]
+    double *blk_energy;       // [step blocks * 8]
     Ctl *ctl;
     // configuration
     float dt;
     int spring_on, steric_on, coulomb_on, hydro_on, imp_on, visc_on;
     int steric_mode, dielectric_mode;
-    float c_steric, c_coulomb, c_hydro;       // cutoffs
-    float lo2_s, hi2_s, lo2_c, hi2_c, lo2_h, hi2_h;  // guard bands on r^2
-    float r2_any;             // squared largest cutoff band end (reject above)
-    float list_radius;        // cutoff + skin of the pair list (grid edge)
-    float list_r2;            // squared, slightly inflated
+    float c_steric, c_coulomb, c_hydro;               // cutoffs
+    float lo2_s, hi2_s, lo2_c, hi2_c, lo2_h, hi2_h;   // guard bands on r^2
+    float list_radius;        // grid edge: largest cutoff + skin
     float half_skin2;         // (skin/2)^2, slightly deflated
     float spring_scale, steric_scale, coulomb_scale, hydro_scale, imp_scale;
-    float dielectric;
     float visc;
     float imp_z0, imp_alpha;
     float k_spring_f;         // (float) kSpringForceConvert
-    float k_elec_e;           // kCoulombEnergyPerA
-    float k_elec_f;           // kElecForceConvert / (4 pi)
+    float k_elec_e;           // kCoulombEnergyPerA / dielectric
+    float k_elec_f;           // kElecForceConvert / (4 pi dielectric)
     float k_kin;              // kKineticConvert
     float k_imp_f;            // kImpForceConvert
     float k_hydro_e;          // N_A * 1e-3

@@ -1,12 +1,20 @@
 // bs_kernels.cu -- sm_103a kernels of BioSpring's per-step force-and-integrate loop.
 //
 // Data layout (all in HBM, structure of arrays, particles in cell-sorted order):
-//   pos[2]   float4 (x, y, z, charge)       double-buffered: a step reads one, writes the other
-//   vel[2]   float4 (vx, vy, vz, 0)
-//   jprm[2]  float4 (steric a, steric b, hydrophobicity, flag bits)  re-laid out at each rebuild
-//   perm[2]  sorted slot -> caller id;  inv: caller id -> sorted slot
-//   se_*     springs of each slot, ELL column-major [k * npad + slot] (coalesced per warp)
-//   pl       nonbonded pair list, ELL column-major [k * npad + slot], rebuilt every K steps
+//   pos[2]    float4 (x, y, z, P)   double-buffered: a step reads one and writes the other
+//   vel[2]    float4 (vx, vy, vz, 0)
+//   fhi/chg/hyd/flags/iprm[2]       per-particle parameters, re-laid out at every rebuild
+//   perm[2]   sorted slot -> caller id;  inv: caller id -> sorted slot
+//   se_*      springs of each slot, ELL column-major [k * npad + slot] (coalesced per warp),
+//             rows ascending by partner slot
+//   pl[t]     typed nonbonded pair lists (steric, Coulomb, hydrophobic), ELL column-major,
+//             entries ascending, rebuilt every K steps from the cell grid
+//
+// Steric factors: the pair parameters of the LJ forms factor per particle,
+// eps_ij r_ij^m = (a_i b_i^m)(a_j b_j^m) with eps_ij = a_i a_j and r_ij = b_i b_j
+// (Amber/Lewitt: a = sqrt(eps), b = sqrt(r), CombinationRules.hpp:18-31; Zacharias: a = eps,
+// b = r), so P = a b^6 and fhi = a b^12 (Amber) or a b^8 (Lewitt, Zacharias); the LJ path
+// then needs only 1/r^2 (no square root, no division).
 //
 // Rebuild (every K steps, or when a particle drifted more than skin/2):
 //   k_bbox -> k_cell_count -> k_cell_scan -> k_cell_place -> k_cell_sort -> k_reorder
@@ -34,10 +42,6 @@ namespace bsg
 namespace
 {
 
-constexpr uint32_t kColMask = 0x3fffffffu;
-constexpr uint32_t kColStatic = 0x80000000u;   // partner is static: the pair's full energy is ours
-constexpr uint32_t kColInactive = 0x40000000u; // spring between two rigid particles: excluded, no force
-
 __device__ __forceinline__ int status_of(const Ctl *c) { return *(volatile const int *)&c->status; }
 
 __device__ __forceinline__ unsigned int f2ord(float f)
@@ -49,6 +53,24 @@ __device__ __forceinline__ float ord2f(unsigned int u)
 {
     const unsigned int b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
     return __uint_as_float(b);
+}
+
+// 1/x: hardware approximation refined by one Newton-Raphson step for f(r) = 1/r - x,
+// r1 = r0 + r0 (1 - x r0); about one unit in the last place for normal x.
+__device__ __forceinline__ float recip_nr(float x)
+{
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return fmaf(r, fmaf(-x, r, 1.0f), r);
+}
+
+// 1/sqrt(x): hardware approximation refined by one Newton-Raphson step for
+// f(r) = 1/r^2 - x, r1 = r0 (3 - x r0^2) / 2.
+__device__ __forceinline__ float rsqrt_nr(float x)
+{
+    float r;
+    asm("rsqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r * fmaf(-0.5f * x, r * r, 1.5f);
 }
 
 // Reference cell coordinate along one axis: (size_t)((x - min) / radius), clamped (nsearch.hpp:282-289).
@@ -64,7 +86,7 @@ __device__ __forceinline__ int ref_cell_coord(float x, double mn, float radius, 
 // distance of the float coordinates (nsearch.hpp:230, measure.hpp:163-169); the force routine
 // then compares the float-rounded FP64 norm of the float difference vector (Particle.cpp:222-224,
 // Vector3f.cpp:9-12, measure.hpp:188-196). Only pairs inside the guard band come here.
-__device__ __noinline__ bool exact_pair_test(float4 pi, float4 pj, float cutoff, bool nonzero, float *dist)
+__device__ __noinline__ bool exact_pair_test(float4 pi, float4 pj, float cutoff, bool nonzero)
 {
     const double ax = __dsub_rn(static_cast<double>(pi.x), static_cast<double>(pj.x));
     const double ay = __dsub_rn(static_cast<double>(pi.y), static_cast<double>(pj.y));
@@ -83,112 +105,26 @@ __device__ __noinline__ bool exact_pair_test(float4 pi, float4 pj, float cutoff,
         return false;
     if (nonzero && !(d != 0.0f))
         return false;
-    *dist = d;
     return true;
 }
 
 // Classifies a pair for one term. Outside the band [lo2, hi2) the FP32 squared distance decides
 // (its error is far below the band); inside it, and for (near-)coincident particles, the exact
-// reference test decides. Returns true if the pair interacts and sets d.
-__device__ __forceinline__ bool pair_in(float r2, float lo2, float hi2, float4 pi, float4 pj, float cutoff, bool nonzero,
-                                        float *d)
+// reference test decides.
+__device__ __forceinline__ bool pair_in(float r2, float lo2, float hi2, float4 pi, float4 pj, float cutoff,
+                                        bool nonzero)
 {
     if (r2 >= hi2)
         return false;
     if (r2 < lo2 && r2 > 1e-20f)
-    {
-        *d = sqrtf(r2);
         return true;
-    }
-    return exact_pair_test(pi, pj, cutoff, nonzero, d);
-}
-
-// Steric force module and pair energy (energy/steric.hpp:27-156, scale applied by the caller).
-// a, b are the per-particle factors: Amber/Lewitt sqrt(eps), sqrt(radius); Zacharias eps, radius;
-// linear: b = radius.
-template <int SM>
-__device__ __forceinline__ void steric_pair(float d, float inv_d, float ai, float bi, float aj, float bj, float kf,
-                                            float &fm, float &e)
-{
-    if (SM == BS_STERIC_LINEAR)
-    {
-        const float dv = d - (bi + bj);
-        if (dv > 0.0f)
-        {
-            fm = 0.0f;
-            e = 0.0f;
-        }
-        else
-        {
-            e = 0.5f * dv * dv;
-            fm = -fabsf(dv) * kf;
-        }
-    }
-    else
-    {
-        if (d < 0.1f)
-        {
-            fm = 0.0f;
-            e = 0.0f;
-            return;
-        }
-        const float eij = ai * aj;
-        const float sr = (bi * bj) * inv_d;
-        const float s2 = sr * sr;
-        const float s6 = s2 * s2 * s2;
-        if (SM == BS_STERIC_LJ_12_6_AMBER)
-        {
-            const float s12 = s6 * s6;
-            e = eij * (s12 - 2.0f * s6);
-            fm = 12.0f * eij * inv_d * (s6 - s12) * kf;
-        }
-        else if (SM == BS_STERIC_LJ_8_6_LEWITT)
-        {
-            const float s8 = s6 * s2;
-            e = eij * (3.0f * s8 - 4.0f * s6);
-            fm = 24.0f * eij * inv_d * (s6 - s8) * kf;
-        }
-        else
-        {
-            const float s8 = s6 * s2;
-            e = eij * (s8 - s6);
-            fm = eij * inv_d * (6.0f * s6 - 8.0f * s8) * kf;
-        }
-    }
-}
-
-// Coulomb force module and energy (energy/electrostatic.hpp:16-49); with the distance-dependent
-// dielectric eps = D r the energy is K q q / (D r^2) and the module is -dE/dr.
-__device__ __forceinline__ void coulomb_pair(const Params &p, float d, float inv_d, float qq, float &fm, float &e)
-{
-    if (d < 0.001f)
-    {
-        fm = 0.0f;
-        e = 0.0f;
-        return;
-    }
-    const float invD = 1.0f / p.dielectric;
-    if (p.dielectric_mode == BS_DIELECTRIC_DISTANCE)
-    {
-        const float t = qq * inv_d * inv_d * invD;
-        e = p.k_elec_e * t;
-        fm = -2.0f * p.k_elec_f * t * inv_d;
-    }
-    else
-    {
-        const float t = qq * inv_d * invD;
-        e = p.k_elec_e * t;
-        fm = -p.k_elec_f * t * inv_d;
-    }
-    e *= p.coulomb_scale;
-    fm *= p.coulomb_scale;
+    return exact_pair_test(pi, pj, cutoff, nonzero);
 }
 
 // Block-wide FP64 reduction of NE per-thread float partials into the block's slot of
 // blk_energy; the last block to finish sums every block's partials in block order.
 template <int NE, int BLOCK>
-__device__ __forceinline__ bool reduce_energies(const float (&e)[NE], double *blk, Ctl *ctl, unsigned int *done,
-                                                double *dst, bool accumulate_first)
+__device__ __forceinline__ bool reduce_energies(const float (&e)[NE], double *blk, unsigned int *done, double *dst)
 {
     __shared__ double sh[NE][BLOCK / 32];
     __shared__ bool am_last;
@@ -219,7 +155,6 @@ __device__ __forceinline__ bool reduce_energies(const float (&e)[NE], double *bl
     if (!am_last)
         return false;
     __threadfence();
-    // Last block: fixed-order sum over blocks.
     for (int k = 0; k < NE; ++k)
     {
         double v = 0.0;
@@ -237,10 +172,7 @@ __device__ __forceinline__ bool reduce_energies(const float (&e)[NE], double *bl
             double t = 0.0;
             for (int w = 0; w < BLOCK / 32; ++w)
                 t += sh[0][w];
-            if (accumulate_first && k == 0)
-                dst[k] += t;
-            else
-                dst[k] = t;
+            dst[k] = t;
         }
     }
     if (threadIdx.x == 0)
@@ -258,36 +190,39 @@ __global__ void __launch_bounds__(kBboxBlock) k_bbox(Params p)
     if (status_of(ctl) & kRebuildBlocking)
         return;
     const float4 *pos = p.pos[ctl->sbuf];
-    float mn0 = FLT_MAX, mn1 = FLT_MAX, mn2 = FLT_MAX, mx0 = -FLT_MAX, mx1 = -FLT_MAX, mx2 = -FLT_MAX;
+    float v[6] = {FLT_MAX, FLT_MAX, FLT_MAX, FLT_MAX, FLT_MAX, FLT_MAX}; // min x,y,z and -max x,y,z
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x)
     {
         const float4 q = pos[i];
-        mn0 = fminf(mn0, q.x);
-        mn1 = fminf(mn1, q.y);
-        mn2 = fminf(mn2, q.z);
-        mx0 = fmaxf(mx0, q.x);
-        mx1 = fmaxf(mx1, q.y);
-        mx2 = fmaxf(mx2, q.z);
+        v[0] = fminf(v[0], q.x);
+        v[1] = fminf(v[1], q.y);
+        v[2] = fminf(v[2], q.z);
+        v[3] = fminf(v[3], -q.x);
+        v[4] = fminf(v[4], -q.y);
+        v[5] = fminf(v[5], -q.z);
     }
+    __shared__ float sh[6][kBboxBlock / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
+    for (int k = 0; k < 6; ++k)
     {
-        mn0 = fminf(mn0, __shfl_down_sync(0xffffffffu, mn0, o));
-        mn1 = fminf(mn1, __shfl_down_sync(0xffffffffu, mn1, o));
-        mn2 = fminf(mn2, __shfl_down_sync(0xffffffffu, mn2, o));
-        mx0 = fmaxf(mx0, __shfl_down_sync(0xffffffffu, mx0, o));
-        mx1 = fmaxf(mx1, __shfl_down_sync(0xffffffffu, mx1, o));
-        mx2 = fmaxf(mx2, __shfl_down_sync(0xffffffffu, mx2, o));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v[k] = fminf(v[k], __shfl_down_sync(0xffffffffu, v[k], o));
+        if (lane == 0)
+            sh[k][warp] = v[k];
     }
+    __syncthreads();
     unsigned int *enc = ctl->bbox_enc;
-    if ((threadIdx.x & 31) == 0)
+    if (threadIdx.x < 6)
     {
-        atomicMin(&enc[0], f2ord(mn0));
-        atomicMin(&enc[1], f2ord(mn1));
-        atomicMin(&enc[2], f2ord(mn2));
-        atomicMax(&enc[3], f2ord(mx0));
-        atomicMax(&enc[4], f2ord(mx1));
-        atomicMax(&enc[5], f2ord(mx2));
+        float m = sh[threadIdx.x][0];
+        for (int w = 1; w < kBboxBlock / 32; ++w)
+            m = fminf(m, sh[threadIdx.x][w]);
+        if (threadIdx.x < 3)
+            atomicMin(&enc[threadIdx.x], f2ord(m));
+        else
+            atomicMax(&enc[threadIdx.x], f2ord(-m));
     }
     __threadfence();
     __syncthreads();
@@ -442,7 +377,10 @@ __global__ void __launch_bounds__(kBuildBlock) k_reorder(Params p)
         const float4 q = p.pos[sb][old];
         p.pos[sb ^ 1][i] = q;
         p.vel[sb ^ 1][i] = p.vel[sb][old];
-        p.jprm[lb ^ 1][i] = p.jprm[lb][old];
+        p.fhi[lb ^ 1][i] = p.fhi[lb][old];
+        p.chg[lb ^ 1][i] = p.chg[lb][old];
+        p.hyd[lb ^ 1][i] = p.hyd[lb][old];
+        p.flags[lb ^ 1][i] = p.flags[lb][old];
         p.iprm[lb ^ 1][i] = p.iprm[lb][old];
         p.pos_build[i] = q;
         p.inv[id] = i;
@@ -461,7 +399,8 @@ __global__ void __launch_bounds__(kBuildBlock) k_reorder(Params p)
     }
 }
 
-// Springs of every slot in the new layout, partners as slots (ELL, column-major).
+// Springs of every slot in the new layout, partners as slots (ELL, column-major), each row
+// sorted by partner slot so that the pair-list build can exclude bonded pairs by a merge.
 __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
 {
     Ctl *ctl = p.ctl;
@@ -477,21 +416,39 @@ __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
     }
     const int id = p.perm[ctl->lbuf][s];
     const int r0 = p.sp_row[id], r1 = p.sp_row[id + 1];
+    const size_t stride = static_cast<size_t>(p.npad);
     for (int e = r0; e < r1; ++e)
     {
-        const uint32_t c = static_cast<uint32_t>(p.sp_col[e]);
-        const uint32_t slot = static_cast<uint32_t>(p.inv[c & kColMask]);
-        const size_t at = static_cast<size_t>(e - r0) * p.npad + s;
-        p.se_col[at] = static_cast<int>(slot | (c & ~kColMask));
-        p.se_k[at] = p.sp_k[e];
-        p.se_r0[at] = p.sp_r0[e];
+        const unsigned int c = p.sp_col[e];
+        const unsigned int slot = static_cast<unsigned int>(p.inv[c & kSlotMask]);
+        const unsigned int val = slot | (c & ~kSlotMask);
+        const float kk = p.sp_k[e], rr = p.sp_r0[e];
+        // insertion into the sorted row [0, e - r0)
+        int at = e - r0;
+        while (at > 0)
+        {
+            const size_t prev = static_cast<size_t>(at - 1) * stride + s;
+            const unsigned int pv = p.se_col[prev];
+            if ((pv & kSlotMask) <= slot)
+                break;
+            const size_t cur = static_cast<size_t>(at) * stride + s;
+            p.se_col[cur] = pv;
+            p.se_k[cur] = p.se_k[prev];
+            p.se_r0[cur] = p.se_r0[prev];
+            --at;
+        }
+        const size_t dst = static_cast<size_t>(at) * stride + s;
+        p.se_col[dst] = val;
+        p.se_k[dst] = kk;
+        p.se_r0[dst] = rr;
     }
     p.se_deg[s] = r1 - r0;
 }
 
-// Pair list of every dynamic slot: all slots within the list radius (cutoff + skin) found in
-// the 27 neighbouring cells, minus the slot itself and, when springs are enabled, its spring
-// partners (Particle.cpp:213-218). Entries come out in increasing slot order.
+// Typed pair lists of every dynamic slot from the 27 neighbouring cells: steric (all pairs
+// within its cutoff + skin), Coulomb (both charged) and hydrophobic (both hydrophobic),
+// minus the slot itself and, when springs are enabled, its spring partners
+// (Particle.cpp:213-218), found by a merge with the sorted spring row. Entries ascend.
 __global__ void __launch_bounds__(kBuildBlock) k_pairlist(Params p)
 {
     Ctl *ctl = p.ctl;
@@ -502,96 +459,303 @@ __global__ void __launch_bounds__(kBuildBlock) k_pairlist(Params p)
         return;
     if (s >= p.n)
     {
-        p.pl_cnt[s] = 0;
+        for (int t = 0; t < kTerms; ++t)
+            p.pl[t].cnt[s] = 0;
         return;
     }
     const int sb = ctl->sbuf, lb = ctl->lbuf;
-    const float4 *pos = p.pos[sb];
-    const float4 *jp = p.jprm[lb];
-    const uint32_t fi = __float_as_uint(jp[s].w);
+    const float4 *__restrict__ pos = p.pos[sb];
+    const unsigned int *__restrict__ fl = p.flags[lb];
+    const unsigned int fi = fl[s];
     if (fi & PF_STATIC)
     {
-        p.pl_cnt[s] = 0;
+        for (int t = 0; t < kTerms; ++t)
+            p.pl[t].cnt[s] = 0;
         return;
     }
     const float4 pi = pos[s];
     const int nx = ctl->gnx, ny = ctl->gny, nz = ctl->gnz;
     const int c = p.cell_of[s];
     const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
-    const int deg = p.se_deg[s];
-    int cnt = 0;
-    const bool need_flags = !p.steric_on;
-    for (int dz = -1; dz <= 1; ++dz)
+    const size_t stride = static_cast<size_t>(p.npad);
+    const bool on0 = p.pl[0].on;
+    const bool on1 = p.pl[1].on && (fi & PF_CHARGED);
+    const bool on2 = p.pl[2].on && (fi & PF_HYDROPHOBIC);
+    const float r2_0 = p.pl[0].r2, r2_1 = p.pl[1].r2, r2_2 = p.pl[2].r2;
+    float r2max = 0.0f;
+    if (on0)
+        r2max = fmaxf(r2max, r2_0);
+    if (on1)
+        r2max = fmaxf(r2max, r2_1);
+    if (on2)
+        r2max = fmaxf(r2max, r2_2);
+    const int deg = p.spring_on ? p.se_deg[s] : 0;
+    int bp = 0;
+    unsigned int nb = deg > 0 ? (p.se_col[s] & kSlotMask) : 0xffffffffu;
+    int cnt0 = 0, cnt1 = 0, cnt2 = 0;
+    const int cap0 = p.pl[0].cap, cap1 = p.pl[1].cap, cap2 = p.pl[2].cap;
+    if (on0 || on1 || on2)
     {
-        const int z = cz + dz;
-        if (z < 0 || z >= nz)
-            continue;
-        for (int dy = -1; dy <= 1; ++dy)
+        for (int dz = -1; dz <= 1; ++dz)
         {
-            const int y = cy + dy;
-            if (y < 0 || y >= ny)
+            const int z = cz + dz;
+            if (z < 0 || z >= nz)
                 continue;
-            const int xa = max(cx - 1, 0), xb = min(cx + 1, nx - 1);
-            const int base = (z * ny + y) * nx;
-            const int j0 = p.cell_start[base + xa], j1 = p.cell_start[base + xb + 1];
-            for (int j = j0; j < j1; ++j)
+            for (int dy = -1; dy <= 1; ++dy)
             {
-                if (j == s)
+                const int y = cy + dy;
+                if (y < 0 || y >= ny)
                     continue;
-                const float4 pj = pos[j];
-                const float dx = pj.x - pi.x, dy2 = pj.y - pi.y, dz2 = pj.z - pi.z;
-                const float r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
-                if (!(r2 < p.list_r2))
-                    continue;
-                if (need_flags)
+                const int xa = max(cx - 1, 0), xb = min(cx + 1, nx - 1);
+                const int base = (z * ny + y) * nx;
+                const int j0 = p.cell_start[base + xa], j1 = p.cell_start[base + xb + 1];
+                for (int j = j0; j < j1; ++j)
                 {
-                    const uint32_t fj = __float_as_uint(jp[j].w);
-                    const bool cc = p.coulomb_on && (fi & PF_CHARGED) && (fj & PF_CHARGED);
-                    const bool hh = p.hydro_on && (fi & PF_HYDROPHOBIC) && (fj & PF_HYDROPHOBIC);
-                    if (!cc && !hh)
+                    if (j == s)
                         continue;
-                }
-                if (p.spring_on)
-                {
-                    bool bonded = false;
-                    for (int k = 0; k < deg; ++k)
-                        if ((static_cast<uint32_t>(p.se_col[static_cast<size_t>(k) * p.npad + s]) & kColMask) ==
-                            static_cast<uint32_t>(j))
+                    const float4 pj = pos[j];
+                    const float dx = pj.x - pi.x, dy2 = pj.y - pi.y, dz2 = pj.z - pi.z;
+                    const float r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
+                    if (!(r2 < r2max))
+                        continue;
+                    if (deg)
+                    {
+                        while (nb < static_cast<unsigned int>(j))
                         {
-                            bonded = true;
-                            break;
+                            ++bp;
+                            nb = bp < deg ? (p.se_col[static_cast<size_t>(bp) * stride + s] & kSlotMask) : 0xffffffffu;
                         }
-                    if (bonded)
-                        continue;
+                        if (nb == static_cast<unsigned int>(j))
+                            continue;
+                    }
+                    const unsigned int fj = fl[j];
+                    const unsigned int entry = static_cast<unsigned int>(j) | ((fj & PF_STATIC) ? kEntryStatic : 0u);
+                    if (on0 && r2 < r2_0)
+                    {
+                        if (cnt0 < cap0)
+                            p.pl[0].idx[static_cast<size_t>(cnt0) * stride + s] = entry;
+                        ++cnt0;
+                    }
+                    if (on1 && (fj & PF_CHARGED) && r2 < r2_1)
+                    {
+                        if (cnt1 < cap1)
+                            p.pl[1].idx[static_cast<size_t>(cnt1) * stride + s] = entry;
+                        ++cnt1;
+                    }
+                    if (on2 && (fj & PF_HYDROPHOBIC) && r2 < r2_2)
+                    {
+                        if (cnt2 < cap2)
+                            p.pl[2].idx[static_cast<size_t>(cnt2) * stride + s] = entry;
+                        ++cnt2;
+                    }
                 }
-                if (cnt < p.pl_cap)
-                    p.pl[static_cast<size_t>(cnt) * p.npad + s] = j;
-                ++cnt;
             }
         }
     }
-    if (cnt > p.pl_cap)
+    const int cnts[3] = {cnt0, cnt1, cnt2};
+    const int caps[3] = {cap0, cap1, cap2};
+    for (int t = 0; t < kTerms; ++t)
     {
-        atomicOr(&ctl->status, ST_PAIR_CAPACITY);
-        atomicMax(&ctl->max_row, cnt);
-        cnt = p.pl_cap;
+        int k = cnts[t];
+        if (k > caps[t])
+        {
+            atomicOr(&ctl->status, ST_PAIR_CAPACITY);
+            atomicMax(&ctl->max_row[t], k);
+            k = caps[t];
+        }
+        p.pl[t].cnt[s] = k;
     }
-    p.pl_cnt[s] = cnt;
 }
 
 // ------------------------------------------------------------------------------------------
 // Step kernel
 // ------------------------------------------------------------------------------------------
 
+// Springs of slot s (Spring.cpp:20-34, spring.hpp:17-29). Returns the force before the unit
+// conversion and scale, and the weighted energy before the scale.
+__device__ __forceinline__ void spring_forces(const Params &p, int s, float4 pi, const float4 *__restrict__ pos,
+                                              float &fx, float &fy, float &fz, float &e)
+{
+    const int deg = p.se_deg[s];
+    const size_t stride = static_cast<size_t>(p.npad);
+    for (int k = 0; k < deg; ++k)
+    {
+        const size_t at = static_cast<size_t>(k) * stride + s;
+        const unsigned int c = __ldg(&p.se_col[at]);
+        if (c & kEntryInactive)
+            continue;
+        const float4 pj = __ldg(&pos[c & kSlotMask]);
+        const float kk = __ldg(&p.se_k[at]), r0 = __ldg(&p.se_r0[at]);
+        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float inv = r2 > 0.0f ? rsqrt_nr(r2) : 0.0f;
+        const float len = r2 * inv;
+        const float dv = len - r0;
+        const float w = (c & kEntryStatic) ? 1.0f : 0.5f;
+        e = fmaf(w * 0.5f * kk, dv * dv, e);
+        const float fod = kk * dv * inv;
+        fx = fmaf(dx, fod, fx);
+        fy = fmaf(dy, fod, fy);
+        fz = fmaf(dz, fod, fz);
+    }
+}
+
+// Steric pairs of slot s (Particle.cpp:368-429, steric.hpp:27-156). The loop is
+// software-pipelined: the next entry and its position are loaded before the current pair
+// is evaluated.
+template <int SM>
+__device__ __forceinline__ void steric_forces(const Params &p, int s, float4 pi, float fhi_i,
+                                              const float4 *__restrict__ pos, const float *__restrict__ fhi,
+                                              float &fx, float &fy, float &fz, float &e)
+{
+    const PairList &L = p.pl[0];
+    const int cnt = L.cnt[s];
+    if (cnt <= 0)
+        return;
+    const size_t stride = static_cast<size_t>(p.npad);
+    const unsigned int *__restrict__ idx = L.idx + s;
+    const float lo2 = p.lo2_s, hi2 = p.hi2_s;
+    unsigned int jn = __ldg(idx);
+    float4 pn = __ldg(&pos[jn & kSlotMask]);
+    for (int k = 0; k < cnt; ++k)
+    {
+        const unsigned int j = jn;
+        const float4 pj = pn;
+        if (k + 1 < cnt)
+        {
+            jn = __ldg(idx + static_cast<size_t>(k + 1) * stride);
+            pn = __ldg(&pos[jn & kSlotMask]);
+        }
+        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 >= hi2)
+            continue;
+        if (!(r2 < lo2 && r2 > 1e-20f) && !exact_pair_test(pi, pj, p.c_steric, false))
+            continue;
+        const float w = (j & kEntryStatic) ? 1.0f : 0.5f;
+        if (SM == BS_STERIC_LINEAR)
+        {
+            // steric.hpp:37-59: E = (d - (ri + rj))^2 / 2 when overlapping, |F| = |d - (ri + rj)|
+            const float inv = r2 > 0.0f ? rsqrt_nr(r2) : 0.0f;
+            const float d = r2 * inv;
+            const float dv = d - (pi.w + pj.w);
+            if (dv > 0.0f)
+                continue;
+            e = fmaf(w * 0.5f, dv * dv, e);
+            const float fod = dv * inv; // -|dv| / d
+            fx = fmaf(dx, fod, fx);
+            fy = fmaf(dy, fod, fy);
+            fz = fmaf(dz, fod, fz);
+        }
+        else
+        {
+            if (r2 < 0.01f) // d < 0.1 A: the LJ forms give zero (steric.hpp:71-72)
+                continue;
+            const float inv2 = recip_nr(r2);
+            const float i6 = inv2 * inv2 * inv2;
+            const float t6 = pi.w * pj.w * i6;
+            const float hj = __ldg(&fhi[j & kSlotMask]);
+            float fod;
+            if (SM == BS_STERIC_LJ_12_6_AMBER)
+            {
+                const float t12 = fhi_i * hj * i6 * i6;
+                e = fmaf(w, t12 - 2.0f * t6, e);
+                fod = 12.0f * (t6 - t12) * inv2;
+            }
+            else if (SM == BS_STERIC_LJ_8_6_LEWITT)
+            {
+                const float t8 = fhi_i * hj * i6 * inv2;
+                e = fmaf(w, 3.0f * t8 - 4.0f * t6, e);
+                fod = 24.0f * (t6 - t8) * inv2;
+            }
+            else
+            {
+                const float t8 = fhi_i * hj * i6 * inv2;
+                e = fmaf(w, t8 - t6, e);
+                fod = (6.0f * t6 - 8.0f * t8) * inv2;
+            }
+            fx = fmaf(dx, fod, fx);
+            fy = fmaf(dy, fod, fy);
+            fz = fmaf(dz, fod, fz);
+        }
+    }
+}
+
+// Coulomb pairs of a charged slot (Particle.cpp:191-253, electrostatic.hpp:16-49). With the
+// distance-dependent dielectric eps = D r, E = K q q / (D r^2) and F = -dE/dr.
+__device__ __forceinline__ void coulomb_forces(const Params &p, int s, float4 pi, float qi,
+                                               const float4 *__restrict__ pos, const float *__restrict__ chg,
+                                               float &fx, float &fy, float &fz, float &e)
+{
+    const PairList &L = p.pl[1];
+    const int cnt = L.cnt[s];
+    const size_t stride = static_cast<size_t>(p.npad);
+    const bool dist = p.dielectric_mode == BS_DIELECTRIC_DISTANCE;
+    for (int k = 0; k < cnt; ++k)
+    {
+        const unsigned int j = __ldg(L.idx + static_cast<size_t>(k) * stride + s);
+        const float4 pj = __ldg(&pos[j & kSlotMask]);
+        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (!pair_in(r2, p.lo2_c, p.hi2_c, pi, pj, p.c_coulomb, true))
+            continue;
+        if (r2 < 1e-6f) // d < 0.001 A gives zero (electrostatic.hpp:18-19)
+            continue;
+        const float inv = rsqrt_nr(r2);
+        const float qq = qi * __ldg(&chg[j & kSlotMask]);
+        const float w = (j & kEntryStatic) ? 1.0f : 0.5f;
+        float t = qq * inv;
+        float fod;
+        if (dist)
+        {
+            t *= inv;
+            fod = -2.0f * t * inv * inv;
+        }
+        else
+            fod = -t * inv * inv;
+        e = fmaf(w, t, e);
+        fx = fmaf(dx, fod, fx);
+        fy = fmaf(dy, fod, fy);
+        fz = fmaf(dz, fod, fz);
+    }
+}
+
+// Hydrophobic pairs (Particle.cpp:269-330, hydrophobic.hpp:20-39).
+__device__ __forceinline__ void hydro_forces(const Params &p, int s, float4 pi, float hi,
+                                             const float4 *__restrict__ pos, const float *__restrict__ hyd,
+                                             float &fx, float &fy, float &fz, float &e)
+{
+    const PairList &L = p.pl[2];
+    const int cnt = L.cnt[s];
+    const size_t stride = static_cast<size_t>(p.npad);
+    for (int k = 0; k < cnt; ++k)
+    {
+        const unsigned int j = __ldg(L.idx + static_cast<size_t>(k) * stride + s);
+        const float4 pj = __ldg(&pos[j & kSlotMask]);
+        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (!pair_in(r2, p.lo2_h, p.hi2_h, pi, pj, p.c_hydro, true))
+            continue;
+        const float inv = rsqrt_nr(r2);
+        const float d = r2 * inv;
+        const float x = hi * __ldg(&hyd[j & kSlotMask]) * expf(-d);
+        const float w = (j & kEntryStatic) ? 1.0f : 0.5f;
+        e = fmaf(-w, x, e);
+        const float fod = x * inv;
+        fx = fmaf(dx, fod, fx);
+        fy = fmaf(dy, fod, fy);
+        fz = fmaf(dz, fod, fz);
+    }
+}
+
 template <int MODE, int SM>
-__global__ void __launch_bounds__(kStepBlock) k_step(Params p)
+__global__ void __launch_bounds__(kStepBlock, kStepMinBlocks) k_step(Params p)
 {
     Ctl *ctl = p.ctl;
     if (status_of(ctl) != 0)
         return;
     const int sb = ctl->sbuf, lb = ctl->lbuf;
     const float4 *__restrict__ pos = p.pos[sb];
-    const float4 *__restrict__ jp = p.jprm[lb];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
 
     // energies: spring, steric, coulomb, hydrophobic, imp, kinetic
@@ -600,9 +764,7 @@ __global__ void __launch_bounds__(kStepBlock) k_step(Params p)
     if (s < p.n)
     {
         const float4 pi = pos[s];
-        const float4 ai = jp[s];
-        const uint32_t fi = __float_as_uint(ai.w);
-        const int id = p.perm[lb][s];
+        const unsigned int fi = p.flags[lb][s];
         if (fi & PF_STATIC)
         {
             if (MODE == MODE_STEP)
@@ -611,97 +773,49 @@ __global__ void __launch_bounds__(kStepBlock) k_step(Params p)
                 p.vel[sb ^ 1][s] = p.vel[sb][s];
             }
             else
-                p.force_out[id] = make_float4(0.f, 0.f, 0.f, 0.f);
+                p.force_out[p.perm[lb][s]] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         else
         {
             float fx = 0.f, fy = 0.f, fz = 0.f;
-            // ---- springs (Spring.cpp:20-34) ----
             if (p.spring_on)
             {
-                const int deg = p.se_deg[s];
-                for (int k = 0; k < deg; ++k)
-                {
-                    const size_t at = static_cast<size_t>(k) * p.npad + s;
-                    const uint32_t c = static_cast<uint32_t>(__ldg(&p.se_col[at]));
-                    if (c & kColInactive)
-                        continue;
-                    const float4 pj = pos[c & kColMask];
-                    const float kk = __ldg(&p.se_k[at]), r0 = __ldg(&p.se_r0[at]);
-                    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                    const float len = sqrtf(dx * dx + dy * dy + dz * dz);
-                    const float dv = len - r0;
-                    const float w = (c & kColStatic) ? 1.0f : 0.5f;
-                    e[0] += w * (0.5f * kk * dv * dv);
-                    const float fm = kk * dv * p.k_spring_f;
-                    const float inv = len > 1e-40f ? 1.0f / len : 0.0f;
-                    fx += dx * inv * fm;
-                    fy += dy * inv * fm;
-                    fz += dz * inv * fm;
-                }
-                e[0] *= p.spring_scale;
-                fx *= p.spring_scale;
-                fy *= p.spring_scale;
-                fz *= p.spring_scale;
+                float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+                spring_forces(p, s, pi, pos, sx, sy, sz, es);
+                const float kf = p.k_spring_f * p.spring_scale;
+                fx = sx * kf;
+                fy = sy * kf;
+                fz = sz * kf;
+                e[0] = es * p.spring_scale;
             }
-            // ---- nonbonded pairs (Particle.cpp:191-253, 269-330, 368-429) ----
+            if (p.steric_on)
             {
-                float sfx = 0.f, sfy = 0.f, sfz = 0.f, es = 0.f;
-                float cfx = 0.f, cfy = 0.f, cfz = 0.f, ec = 0.f;
-                float hfx = 0.f, hfy = 0.f, hfz = 0.f, eh = 0.f;
-                const int cnt = p.pl_cnt[s];
-                const bool qi_on = p.coulomb_on && (fi & PF_CHARGED);
-                const bool hi_on = p.hydro_on && (fi & PF_HYDROPHOBIC);
-                for (int k = 0; k < cnt; ++k)
-                {
-                    const int j = __ldg(&p.pl[static_cast<size_t>(k) * p.npad + s]);
-                    const float4 pj = pos[j];
-                    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                    const float r2 = dx * dx + dy * dy + dz * dz;
-                    if (r2 >= p.r2_any)
-                        continue;
-                    const float4 aj = jp[j];
-                    const uint32_t fj = __float_as_uint(aj.w);
-                    const float w = (fj & PF_STATIC) ? 1.0f : 0.5f;
-                    float d;
-                    if (p.steric_on && pair_in(r2, p.lo2_s, p.hi2_s, pi, pj, p.c_steric, false, &d))
-                    {
-                        const float inv_d = d > 1e-40f ? 1.0f / d : 0.0f;
-                        float fm, pe;
-                        steric_pair<SM>(d, inv_d, ai.x, ai.y, aj.x, aj.y, p.k_spring_f, fm, pe);
-                        es += w * pe;
-                        sfx += dx * inv_d * fm;
-                        sfy += dy * inv_d * fm;
-                        sfz += dz * inv_d * fm;
-                    }
-                    if (qi_on && pj.w != 0.0f && pair_in(r2, p.lo2_c, p.hi2_c, pi, pj, p.c_coulomb, true, &d))
-                    {
-                        const float inv_d = 1.0f / d;
-                        float fm, pe;
-                        coulomb_pair(p, d, inv_d, pi.w * pj.w, fm, pe);
-                        ec += w * pe;
-                        cfx += dx * inv_d * fm;
-                        cfy += dy * inv_d * fm;
-                        cfz += dz * inv_d * fm;
-                    }
-                    if (hi_on && aj.z != 0.0f && pair_in(r2, p.lo2_h, p.hi2_h, pi, pj, p.c_hydro, true, &d))
-                    {
-                        const float inv_d = 1.0f / d;
-                        const float x = ai.z * aj.z * expf(-d);
-                        const float pe = -x * p.k_hydro_e * p.hydro_scale;
-                        const float fm = x * p.k_spring_f * p.hydro_scale;
-                        eh += w * pe;
-                        hfx += dx * inv_d * fm;
-                        hfy += dy * inv_d * fm;
-                        hfz += dz * inv_d * fm;
-                    }
-                }
+                float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+                steric_forces<SM>(p, s, pi, p.fhi[lb][s], pos, p.fhi[lb], sx, sy, sz, es);
+                const float kf = p.k_spring_f * p.steric_scale;
+                fx = fmaf(sx, kf, fx);
+                fy = fmaf(sy, kf, fy);
+                fz = fmaf(sz, kf, fz);
                 e[1] = es * p.steric_scale;
-                e[2] = ec;
-                e[3] = eh;
-                fx += sfx * p.steric_scale + cfx + hfx;
-                fy += sfy * p.steric_scale + cfy + hfy;
-                fz += sfz * p.steric_scale + cfz + hfz;
+            }
+            if (p.coulomb_on && (fi & PF_CHARGED))
+            {
+                float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+                coulomb_forces(p, s, pi, p.chg[lb][s], pos, p.chg[lb], sx, sy, sz, es);
+                fx = fmaf(sx, p.k_elec_f, fx);
+                fy = fmaf(sy, p.k_elec_f, fy);
+                fz = fmaf(sz, p.k_elec_f, fz);
+                e[2] = es * p.k_elec_e;
+            }
+            if (p.hydro_on && (fi & PF_HYDROPHOBIC))
+            {
+                float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+                hydro_forces(p, s, pi, p.hyd[lb][s], pos, p.hyd[lb], sx, sy, sz, es);
+                const float kf = p.k_spring_f * p.hydro_scale;
+                fx = fmaf(sx, kf, fx);
+                fy = fmaf(sy, kf, fy);
+                fz = fmaf(sz, kf, fz);
+                e[3] = es * p.k_hydro_e * p.hydro_scale;
             }
             const float4 v = p.vel[sb][s];
             // ---- viscosity (Particle.cpp:80-84) ----
@@ -730,6 +844,7 @@ __global__ void __launch_bounds__(kStepBlock) k_step(Params p)
             // ---- external force (SpringNetwork::setForce, SpringNetwork.cpp:438-442) ----
             if (ctl->ext_pending)
             {
+                const int id = p.perm[lb][s];
                 const float4 xf = p.ext[id];
                 fx += xf.x;
                 fy += xf.y;
@@ -739,7 +854,7 @@ __global__ void __launch_bounds__(kStepBlock) k_step(Params p)
             }
             if (MODE == MODE_FORCES)
             {
-                p.force_out[id] = make_float4(fx, fy, fz, 0.f);
+                p.force_out[p.perm[lb][s]] = make_float4(fx, fy, fz, 0.f);
             }
             else
             {
@@ -768,11 +883,11 @@ __global__ void __launch_bounds__(kStepBlock) k_step(Params p)
             }
         }
     }
-    if (reduce_energies<6, kStepBlock>(e, p.blk_energy, ctl, &ctl->done_step, ctl->energies, false))
+    if (reduce_energies<6, kStepBlock>(e, p.blk_energy, &ctl->done_step, ctl->energies))
     {
         if (threadIdx.x == 0)
         {
-            // energies[] order: kinetic, spring, steric, electrostatic, imp, hydrophobic
+            // energies[] were written in e[] order: spring, steric, coulomb, hydrophobic, imp, kinetic
             const double sp = ctl->energies[0], st = ctl->energies[1], co = ctl->energies[2],
                          hy = ctl->energies[3], im = ctl->energies[4], ki = ctl->energies[5];
             ctl->energies[BS_ENERGY_KINETIC] = ki;
@@ -850,7 +965,7 @@ __global__ void __launch_bounds__(1024) k_diag_cells(Params p, float cutoff, flo
 {
     const Ctl *ctl = p.ctl;
     const float4 *pos = p.pos[ctl->sbuf];
-    const float4 *jp = p.jprm[ctl->lbuf];
+    const unsigned int *fl = p.flags[ctl->lbuf];
     __shared__ float smin[3][32], smax[3][32];
     float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     for (int i = threadIdx.x; i < p.n; i += blockDim.x)
@@ -898,8 +1013,7 @@ __global__ void __launch_bounds__(1024) k_diag_cells(Params p, float cutoff, flo
     for (int s = threadIdx.x; s < p.n; s += blockDim.x)
     {
         const int id = p.perm[ctl->lbuf][s];
-        const uint32_t f = __float_as_uint(jp[s].w);
-        if (need_flag && !(f & need_flag))
+        if (need_flag && !(fl[s] & need_flag))
         {
             out[id] = -1;
             continue;
@@ -922,38 +1036,39 @@ __global__ void __launch_bounds__(kStepBlock) k_diag_pairs(Params p, int term, l
     if (s >= p.n)
         return;
     const float4 *pos = p.pos[ctl->sbuf];
-    const float4 *jp = p.jprm[ctl->lbuf];
-    const uint32_t fi = __float_as_uint(jp[s].w);
+    const unsigned int fi = p.flags[ctl->lbuf][s];
     if (fi & PF_STATIC)
         return;
-    if (term == BS_TERM_STERIC && !p.steric_on)
-        return;
-    if (term == BS_TERM_COULOMB && !(p.coulomb_on && (fi & PF_CHARGED)))
-        return;
-    if (term == BS_TERM_HYDROPHOBIC && !(p.hydro_on && (fi & PF_HYDROPHOBIC)))
+    const PairList &L = p.pl[term];
+    if (!L.on)
         return;
     const float4 pi = pos[s];
     const int idi = p.perm[ctl->lbuf][s];
-    const int cnt = p.pl_cnt[s];
+    const int cnt = L.cnt[s];
+    float lo2 = p.lo2_s, hi2 = p.hi2_s, cut = p.c_steric;
+    if (term == BS_TERM_COULOMB)
+    {
+        lo2 = p.lo2_c;
+        hi2 = p.hi2_c;
+        cut = p.c_coulomb;
+    }
+    else if (term == BS_TERM_HYDROPHOBIC)
+    {
+        lo2 = p.lo2_h;
+        hi2 = p.hi2_h;
+        cut = p.c_hydro;
+    }
     for (int k = 0; k < cnt; ++k)
     {
-        const int j = p.pl[static_cast<size_t>(k) * p.npad + s];
+        const unsigned int e = L.idx[static_cast<size_t>(k) * p.npad + s];
+        const int j = static_cast<int>(e & kSlotMask);
         const float4 pj = pos[j];
-        const uint32_t fj = __float_as_uint(jp[j].w);
         const int idj = p.perm[ctl->lbuf][j];
-        if (!(fj & PF_STATIC) && idj < idi)
+        if (!(e & kEntryStatic) && idj < idi)
             continue;
         const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        float d;
-        bool in;
-        if (term == BS_TERM_STERIC)
-            in = pair_in(r2, p.lo2_s, p.hi2_s, pi, pj, p.c_steric, false, &d);
-        else if (term == BS_TERM_COULOMB)
-            in = (fj & PF_CHARGED) && pair_in(r2, p.lo2_c, p.hi2_c, pi, pj, p.c_coulomb, true, &d);
-        else
-            in = (fj & PF_HYDROPHOBIC) && pair_in(r2, p.lo2_h, p.hi2_h, pi, pj, p.c_hydro, true, &d);
-        if (!in)
+        if (!pair_in(r2, lo2, hi2, pi, pj, cut, term != BS_TERM_STERIC))
             continue;
         const unsigned long long at = atomicAdd(count, 1ull);
         if (at < cap)

@@ -7,6 +7,11 @@ namespace bsg
 {
 
 constexpr int kStepBlock = 128;
+#ifndef BS_STEP_MIN_BLOCKS
+#define BS_STEP_MIN_BLOCKS 8
+#endif
+// resident blocks of 128 threads per SM the step kernel is compiled for (8: at most 64 registers)
+constexpr int kStepMinBlocks = BS_STEP_MIN_BLOCKS;
 constexpr int kBuildBlock = 128;
 constexpr int kBboxBlock = 256;
 constexpr int kMaxEnergyBlocks = 1 << 16;

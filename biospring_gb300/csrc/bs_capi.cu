@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <unordered_set>
@@ -75,7 +76,7 @@ struct bs_sim
     int period_kernels = 0;
     long long launches = 0;
     // growable buffers (pair lists, grid arrays), freed on regrowth
-    unsigned int *pl_idx[kTerms] = {nullptr, nullptr, nullptr};
+    unsigned int *pl_idx[kLists] = {nullptr, nullptr, nullptr, nullptr};
     int *cell_buf[3] = {nullptr, nullptr, nullptr};
     // diagnostics scratch
     long long *diag_out = nullptr;
@@ -163,7 +164,7 @@ int clear_status(bs_sim *s, int bits)
 // Frees the growable buffers (pair lists and grid arrays).
 void free_growable(bs_sim *s)
 {
-    for (int t = 0; t < kTerms; ++t)
+    for (int t = 0; t < kLists; ++t)
     {
         if (s->pl_idx[t])
             cudaFree(s->pl_idx[t]);
@@ -179,12 +180,12 @@ void free_growable(bs_sim *s)
 
 // (Re)allocates the three pair lists and the cell arrays for the given capacities. The stream
 // is idle when this runs (callers synchronise first), so the old buffers can be released.
-int alloc_lists(bs_sim *s, const int caps[kTerms], int cell_cap)
+int alloc_lists(bs_sim *s, const int caps[kLists], int cell_cap)
 {
     Params &p = s->p;
     BS_CUDA(cudaStreamSynchronize(s->stream));
     free_growable(s);
-    for (int t = 0; t < kTerms; ++t)
+    for (int t = 0; t < kLists; ++t)
     {
         const int cap = p.pl[t].on ? std::max(caps[t], 1) : 1;
         BS_CUDA(cudaMalloc(reinterpret_cast<void **>(&s->pl_idx[t]),
@@ -203,9 +204,9 @@ int alloc_lists(bs_sim *s, const int caps[kTerms], int cell_cap)
     return BS_OK;
 }
 
-int current_caps(const bs_sim *s, int caps[kTerms])
+int current_caps(const bs_sim *s, int caps[kLists])
 {
-    for (int t = 0; t < kTerms; ++t)
+    for (int t = 0; t < kLists; ++t)
         caps[t] = s->p.pl[t].cap;
     return 0;
 }
@@ -245,7 +246,7 @@ int rebuild_now(bs_sim *s)
             const long long need = s->ctl_host->ncells_needed;
             if (need > (1ll << 28))
                 return fail(s, BS_E_CAPACITY, "search grid needs more than 2^28 cells (particles spread too far)");
-            int caps[kTerms];
+            int caps[kLists];
             current_caps(s, caps);
             rc = alloc_lists(s, caps, static_cast<int>(need + need / 2 + 64));
             if (rc)
@@ -255,11 +256,21 @@ int rebuild_now(bs_sim *s)
                 return rc;
             continue;
         }
+        if (st & ST_WIDE)
+        {
+            // a neighbour offset left the 16-bit range: switch the steric list to 32-bit entries
+            s->p.pl16 = 0;
+            destroy_graph(s);
+            rc = clear_status(s, ST_WIDE | ST_PAIR_CAPACITY);
+            if (rc)
+                return rc;
+            continue;
+        }
         if (st & ST_PAIR_CAPACITY)
         {
-            int caps[kTerms];
+            int caps[kLists];
             current_caps(s, caps);
-            for (int t = 0; t < kTerms; ++t)
+            for (int t = 0; t < kLists; ++t)
             {
                 const int need = s->ctl_host->max_row[t];
                 if (need > caps[t])
@@ -616,11 +627,11 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     BS_CUDA(s->dev.alloc(&p.se_k, static_cast<size_t>(npad) * maxdeg));
     BS_CUDA(s->dev.alloc(&p.se_r0, static_cast<size_t>(npad) * maxdeg));
     BS_CUDA(s->dev.alloc(&p.se_deg, npad));
-    for (int t = 0; t < kTerms; ++t)
+    for (int t = 0; t < kLists; ++t)
         BS_CUDA(s->dev.alloc(&p.pl[t].cnt, npad));
     BS_CUDA(s->dev.alloc(&p.cell_of, npad));
     BS_CUDA(s->dev.alloc(&p.tmp_perm, npad));
-    s->step_blocks = (p.n + kStepBlock - 1) / kStepBlock;
+    s->step_blocks = static_cast<int>((static_cast<long long>(p.n) * 8 + kStepBlock - 1) / kStepBlock);
     BS_CUDA(s->dev.alloc(&p.blk_energy, static_cast<size_t>(s->step_blocks) * 8));
     BS_CUDA(s->dev.alloc(&p.ctl, 1));
     BS_CUDA(s->dev.alloc(&s->staging, 3 * static_cast<size_t>(n)));
@@ -630,10 +641,15 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
 
     // ---- pair lists: which terms, radii, first capacities from the density ----
     const double skin = c.list_skin;
-    const double cut[kTerms] = {c.steric_cutoff, c.coulomb_cutoff, c.hydrophobicity_cutoff};
-    const int on[kTerms] = {c.steric_enable != 0, c.coulomb_enable != 0, c.hydrophobicity_enable != 0};
+    bool any_static = false;
+    for (int64_t i = 0; i < n; ++i)
+        any_static = any_static || s->is_static[i];
+    const double cut[kLists] = {c.steric_cutoff, c.coulomb_cutoff, c.hydrophobicity_cutoff, c.steric_cutoff};
+    const int on[kLists] = {c.steric_enable != 0, c.coulomb_enable != 0, c.hydrophobicity_enable != 0,
+                            c.steric_enable != 0 && any_static};
     double list_radius = 1e-3;
-    for (int t = 0; t < kTerms; ++t)
+    p.pl16 = 1;
+    for (int t = 0; t < kLists; ++t)
     {
         p.pl[t].on = on[t];
         const double R = static_cast<float>(cut[t]) + skin;
@@ -657,9 +673,9 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     }
     const int cell_cap = static_cast<int>(std::min(2.0 * cells + 1024.0, 2.0e8));
     // first capacity: 1.5x the mean count expected in the list sphere, at least 32
-    int caps[kTerms];
+    int caps[kLists];
     const double density = static_cast<double>(n) / volume;
-    for (int t = 0; t < kTerms; ++t)
+    for (int t = 0; t < kLists; ++t)
     {
         const double R = static_cast<float>(cut[t]) + skin;
         const double expect = density * 4.18879 * R * R * R;
@@ -703,6 +719,13 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     p.imp_on = c.impala_enable != 0;
     p.visc_on = c.viscosity_enable != 0;
     p.steric_mode = c.steric_mode;
+    p.step_lanes = 4;
+    if (const char *env = std::getenv("BS_STEP_LANES"))
+    {
+        const int v = std::atoi(env);
+        if (v == 1 || v == 2 || v == 4 || v == 8)
+            p.step_lanes = v;
+    }
     p.dielectric_mode = c.dielectric_mode;
     p.c_steric = static_cast<float>(c.steric_cutoff);
     p.c_coulomb = static_cast<float>(c.coulomb_cutoff);
@@ -814,7 +837,7 @@ int bs_synchronize(bs_sim *s)
         s->steps_done = h.steps;
         if (h.status & ST_NONFINITE)
             return fail(s, BS_E_NONFINITE, "Found non-finite position (a particle position became NaN or infinite)");
-        if (h.status & (ST_CELL_CAPACITY | ST_PAIR_CAPACITY))
+        if (h.status & (ST_CELL_CAPACITY | ST_PAIR_CAPACITY | ST_WIDE))
         {
             rc = rebuild_now(s); // grows the lists and rebuilds
             if (rc)

@@ -39,6 +39,7 @@ enum : int
     ST_PAIR_CAPACITY = 2,   // a pair-list row overflowed
     ST_CELL_CAPACITY = 4,   // the search grid needs more cells than allocated
     ST_STALE = 8,           // a particle drifted more than half the list skin: rebuild needed
+    ST_WIDE = 16,           // a neighbour offset does not fit the 16-bit steric list
 };
 
 // particle flag bits
@@ -55,7 +56,11 @@ constexpr uint32_t kSlotMask = 0x3fffffffu;
 constexpr uint32_t kEntryStatic = 0x80000000u;   // the partner is static: the pair's full energy is ours
 constexpr uint32_t kEntryInactive = 0x40000000u; // spring between two rigid particles: no force
 
-constexpr int kTerms = 3; // steric, Coulomb, hydrophobic pair lists
+constexpr int kTerms = 3; // nonbonded terms: steric, Coulomb, hydrophobic
+// Pair lists: 0 = steric, dynamic partners (16-bit slot offsets when they fit), 1 = Coulomb,
+// 2 = hydrophobic, 3 = steric, static partners (full pair energy, rare)
+constexpr int kLists = 4;
+constexpr int kListStericStatic = 3;
 
 // Device control block: one per simulation handle, in device memory.
 struct Ctl
@@ -67,7 +72,7 @@ struct Ctl
     unsigned int done_bbox;
     unsigned int done_reorder;
     long long steps;          // completed steps since setup
-    int max_row[kTerms];      // largest pair-list row of each term seen at the last build
+    int max_row[kLists];      // largest row of each pair list seen at the last build
     int ncells_needed;
     // search grid of the current layout (reference formula, nsearch.hpp:342-354)
     double gmin[3];
@@ -79,7 +84,8 @@ struct Ctl
     double energies[8];        // BS_ENERGY_* of the last evaluation
 };
 
-// One typed pair list: ELL, column-major [k * npad + slot], entries = slot | kEntryStatic.
+// One typed pair list, row-major [slot * cap + k]: entries = slot | kEntryStatic, or for
+// list 0 in 16-bit mode, (short)(partner slot - slot).
 struct PairList
 {
     unsigned int *idx;
@@ -121,7 +127,8 @@ struct Params
     float *se_r0;
     int *se_deg;              // [npad]
     // nonbonded pair lists
-    PairList pl[kTerms];
+    PairList pl[kLists];
+    int pl16;                 // list 0 holds 16-bit offsets
     // search grid
     int *cell_of;             // [npad] cell of each sorted slot (new layout)
     int *cell_cnt;            // [cell_cap + 1]
@@ -136,6 +143,7 @@ struct Params
     float dt;
     int spring_on, steric_on, coulomb_on, hydro_on, imp_on, visc_on;
     int steric_mode, dielectric_mode;
+    int step_lanes;           // threads per particle in the step kernel (1, 2, 4 or 8)
     float c_steric, c_coulomb, c_hydro;               // cutoffs
     float lo2_s, hi2_s, lo2_c, hi2_c, lo2_h, hi2_h;   // guard bands on r^2
     float list_radius;        // grid edge: largest cutoff + skin

@@ -7,8 +7,9 @@
 //   perm[2]   sorted slot -> caller id;  inv: caller id -> sorted slot
 //   se_*      springs of each slot, ELL column-major [k * npad + slot] (coalesced per warp),
 //             rows ascending by partner slot
-//   pl[t]     typed nonbonded pair lists (steric, Coulomb, hydrophobic), ELL column-major,
-//             entries ascending, rebuilt every K steps from the cell grid
+//   pl[t]     typed nonbonded pair lists (steric dynamic / static partners, Coulomb,
+//             hydrophobic), row-major [slot * cap + k], entries ascending, rebuilt every K steps
+//             from the cell grid; the steric row holds 16-bit slot offsets when they fit
 //
 // Steric factors: the pair parameters of the LJ forms factor per particle,
 // eps_ij r_ij^m = (a_i b_i^m)(a_j b_j^m) with eps_ij = a_i a_j and r_ij = b_i b_j
@@ -121,31 +122,57 @@ __device__ __forceinline__ bool pair_in(float r2, float lo2, float hi2, float4 p
     return exact_pair_test(pi, pj, cutoff, nonzero);
 }
 
-// Block-wide FP64 reduction of NE per-thread float partials into the block's slot of
-// blk_energy; the last block to finish sums every block's partials in block order.
-template <int NE, int BLOCK>
-__device__ __forceinline__ bool reduce_energies(const float (&e)[NE], double *blk, unsigned int *done, double *dst)
+// Knuth's TwoSum: s = fl(a + b) and s + err == a + b exactly (round-to-nearest, no contraction).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &err)
 {
-    __shared__ double sh[NE][BLOCK / 32];
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (hi, lo) += (h2, l2) in float-float (double-single) arithmetic: about 44 significant bits.
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float h2, float l2)
+{
+    float s, e;
+    two_sum(hi, h2, s, e);
+    e = __fadd_rn(e, __fadd_rn(lo, l2));
+    two_sum(s, e, hi, lo);
+}
+
+// Deterministic reduction of NE per-thread float partials over the grid. Warp sums are FP32
+// trees, block sums float-float (compensated), the block partials are stored as (hi, lo) pairs, and the
+// last block to finish sums them in block order, also float-float, and writes the totals as
+// double. The result carries the accuracy of an FP64 reduction without using the FP64 pipe,
+// which runs at a small fraction of the FP32 rate on this part.
+template <int NE, int BLOCK>
+__device__ __forceinline__ bool reduce_energies(const float (&e)[NE], double *blk_d, unsigned int *done, double *dst)
+{
+    float *blk = reinterpret_cast<float *>(blk_d); // [block][16]: (hi, lo) per energy
+    __shared__ float shh[NE][BLOCK / 32], shl[NE][BLOCK / 32];
     __shared__ bool am_last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < NE; ++k)
     {
-        double v = static_cast<double>(e[k]);
+        // 32 terms: a plain FP32 tree keeps ~1e-7 relative; compensation starts above the warp
+        float v = e[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
             v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0)
-            sh[k][warp] = v;
+        {
+            shh[k][warp] = v;
+            shl[k][warp] = 0.0f;
+        }
     }
     __syncthreads();
     if (threadIdx.x < NE)
     {
-        double v = 0.0;
+        float hi = 0.0f, lo = 0.0f;
         for (int w = 0; w < BLOCK / 32; ++w)
-            v += sh[threadIdx.x][w];
-        blk[static_cast<size_t>(blockIdx.x) * 8 + threadIdx.x] = v;
+            ff_add(hi, lo, shh[threadIdx.x][w], shl[threadIdx.x][w]);
+        blk[static_cast<size_t>(blockIdx.x) * 16 + 2 * threadIdx.x] = hi;
+        blk[static_cast<size_t>(blockIdx.x) * 16 + 2 * threadIdx.x + 1] = lo;
     }
     __threadfence();
     __syncthreads();
@@ -157,22 +184,30 @@ __device__ __forceinline__ bool reduce_energies(const float (&e)[NE], double *bl
     __threadfence();
     for (int k = 0; k < NE; ++k)
     {
-        double v = 0.0;
+        float hi = 0.0f, lo = 0.0f;
         for (unsigned int b = threadIdx.x; b < gridDim.x; b += BLOCK)
-            v += __ldcg(&blk[static_cast<size_t>(b) * 8 + k]);
+            ff_add(hi, lo, __ldcg(&blk[static_cast<size_t>(b) * 16 + 2 * k]),
+                   __ldcg(&blk[static_cast<size_t>(b) * 16 + 2 * k + 1]));
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
-            v += __shfl_down_sync(0xffffffffu, v, o);
+        {
+            const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
+            const float l2 = __shfl_down_sync(0xffffffffu, lo, o);
+            ff_add(hi, lo, h2, l2);
+        }
         __syncthreads();
         if (lane == 0)
-            sh[0][warp] = v;
+        {
+            shh[0][warp] = hi;
+            shl[0][warp] = lo;
+        }
         __syncthreads();
         if (threadIdx.x == 0)
         {
-            double t = 0.0;
+            float th = 0.0f, tl = 0.0f;
             for (int w = 0; w < BLOCK / 32; ++w)
-                t += sh[0][w];
-            dst[k] = t;
+                ff_add(th, tl, shh[0][w], shl[0][w]);
+            dst[k] = static_cast<double>(th) + static_cast<double>(tl);
         }
     }
     if (threadIdx.x == 0)
@@ -399,8 +434,7 @@ __global__ void __launch_bounds__(kBuildBlock) k_reorder(Params p)
     }
 }
 
-// Springs of every slot in the new layout, partners as slots (ELL, column-major), each row
-// sorted by partner slot so that the pair-list build can exclude bonded pairs by a merge.
+// Springs of every slot in the new layout, partners as slots (ELL, column-major).
 __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
 {
     Ctl *ctl = p.ctl;
@@ -421,81 +455,98 @@ __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
     {
         const unsigned int c = p.sp_col[e];
         const unsigned int slot = static_cast<unsigned int>(p.inv[c & kSlotMask]);
-        const unsigned int val = slot | (c & ~kSlotMask);
-        const float kk = p.sp_k[e], rr = p.sp_r0[e];
-        // insertion into the sorted row [0, e - r0)
-        int at = e - r0;
-        while (at > 0)
-        {
-            const size_t prev = static_cast<size_t>(at - 1) * stride + s;
-            const unsigned int pv = p.se_col[prev];
-            if ((pv & kSlotMask) <= slot)
-                break;
-            const size_t cur = static_cast<size_t>(at) * stride + s;
-            p.se_col[cur] = pv;
-            p.se_k[cur] = p.se_k[prev];
-            p.se_r0[cur] = p.se_r0[prev];
-            --at;
-        }
-        const size_t dst = static_cast<size_t>(at) * stride + s;
-        p.se_col[dst] = val;
-        p.se_k[dst] = kk;
-        p.se_r0[dst] = rr;
+        const size_t dst = static_cast<size_t>(e - r0) * stride + s;
+        p.se_col[dst] = slot | (c & ~kSlotMask);
+        p.se_k[dst] = p.sp_k[e];
+        p.se_r0[dst] = p.sp_r0[e];
     }
     p.se_deg[s] = r1 - r0;
 }
 
-// Typed pair lists of every dynamic slot from the 27 neighbouring cells: steric (all pairs
-// within its cutoff + skin), Coulomb (both charged) and hydrophobic (both hydrophobic),
-// minus the slot itself and, when springs are enabled, its spring partners
-// (Particle.cpp:213-218), found by a merge with the sorted spring row. Entries ascend.
-__global__ void __launch_bounds__(kBuildBlock) k_pairlist(Params p)
+// Typed pair lists from the cell grid: steric (every pair within its cutoff + skin, dynamic and
+// static partners apart), Coulomb (both charged) and hydrophobic (both hydrophobic), minus the
+// slot itself and, when springs are enabled, its spring partners (Particle.cpp:213-218).
+//
+// A warp owns a batch of up to kPlBatch home particles of one cell. The candidates of the 27
+// neighbouring cells form nine contiguous x-runs of slots; each run is taken 32 slots at a time,
+// one candidate per lane (coalesced loads). For every home particle of the batch, in turn, the
+// lanes test their candidates, the warp ballots the accepted ones and appends them to the home
+// particle's row-major row at consecutive positions (coalesced stores). Control flow depends
+// only on the home particle, so lanes never diverge; rows come out in ascending slot order.
+// Bonded partners are excluded with the home particle's sorted spring row: only the partners
+// falling in the current 32-slot window are compared. In 16-bit mode the steric row holds
+// partner-minus-slot offsets.
+template <bool PL16>
+__global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
 {
+    constexpr int HB = kPlBatch;
+    __shared__ float4 sh_pi[kPlWarps][HB];
+    __shared__ unsigned int sh_fi[kPlWarps][HB];
+    __shared__ int sh_bp[kPlWarps][HB];
+    __shared__ int sh_deg[kPlWarps][HB];
+    __shared__ int sh_cnt[kPlWarps][kLists][HB];
+    __shared__ int sh_part[kPlWarps][HB][kPlMaxDeg]; // sorted spring partners of the batch
+    __shared__ int blocked;
     Ctl *ctl = p.ctl;
-    if (status_of(ctl) & kRebuildBlocking)
+    if (threadIdx.x == 0)
+        blocked = status_of(ctl) & kRebuildBlocking;
+    __syncthreads();
+    if (blocked)
         return;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= p.npad)
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nx = ctl->gnx, ny = ctl->gny, nz = ctl->gnz;
+    const int gw = blockIdx.x * kPlWarps + wid;
+    const int c = gw / kPlBatchesPerCell;
+    const int b0 = gw % kPlBatchesPerCell;
+    if (c >= nx * ny * nz)
         return;
-    if (s >= p.n)
-    {
-        for (int t = 0; t < kTerms; ++t)
-            p.pl[t].cnt[s] = 0;
+    const int h0 = p.cell_start[c], h1 = p.cell_start[c + 1];
+    if (h0 + b0 * HB >= h1)
         return;
-    }
     const int sb = ctl->sbuf, lb = ctl->lbuf;
     const float4 *__restrict__ pos = p.pos[sb];
     const unsigned int *__restrict__ fl = p.flags[lb];
-    const unsigned int fi = fl[s];
-    if (fi & PF_STATIC)
-    {
-        for (int t = 0; t < kTerms; ++t)
-            p.pl[t].cnt[s] = 0;
-        return;
-    }
-    const float4 pi = pos[s];
-    const int nx = ctl->gnx, ny = ctl->gny, nz = ctl->gnz;
-    const int c = p.cell_of[s];
     const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
-    const size_t stride = static_cast<size_t>(p.npad);
-    const bool on0 = p.pl[0].on;
-    const bool on1 = p.pl[1].on && (fi & PF_CHARGED);
-    const bool on2 = p.pl[2].on && (fi & PF_HYDROPHOBIC);
     const float r2_0 = p.pl[0].r2, r2_1 = p.pl[1].r2, r2_2 = p.pl[2].r2;
-    float r2max = 0.0f;
-    if (on0)
-        r2max = fmaxf(r2max, r2_0);
-    if (on1)
-        r2max = fmaxf(r2max, r2_1);
-    if (on2)
-        r2max = fmaxf(r2max, r2_2);
-    const int deg = p.spring_on ? p.se_deg[s] : 0;
-    int bp = 0;
-    unsigned int nb = deg > 0 ? (p.se_col[s] & kSlotMask) : 0xffffffffu;
-    int cnt0 = 0, cnt1 = 0, cnt2 = 0;
-    const int cap0 = p.pl[0].cap, cap1 = p.pl[1].cap, cap2 = p.pl[2].cap;
-    if (on0 || on1 || on2)
+    const bool l0 = p.pl[0].on, l1 = p.pl[1].on, l2 = p.pl[2].on;
+    const size_t stride = static_cast<size_t>(p.npad);
+    const unsigned int below = (1u << lane) - 1u;
+    for (int hb = h0 + b0 * HB; hb < h1; hb += HB * kPlBatchesPerCell)
     {
+        const int nh = min(HB, h1 - hb);
+        __syncwarp();
+        if (lane < nh)
+        {
+            sh_pi[wid][lane] = pos[hb + lane];
+            sh_fi[wid][lane] = fl[hb + lane];
+            sh_bp[wid][lane] = 0;
+            sh_deg[wid][lane] = p.spring_on ? p.se_deg[hb + lane] : 0;
+            for (int q = 0; q < kLists; ++q)
+                sh_cnt[wid][q][lane] = 0;
+        }
+        __syncwarp();
+        // spring partners of each home particle, sorted ascending (rank sort across the warp)
+        for (int ii = 0; ii < nh; ++ii)
+        {
+            const int deg = sh_deg[wid][ii];
+            if (deg > kPlMaxDeg)
+                continue; // scanned from global memory below
+            const int i = hb + ii;
+            for (int k0 = 0; k0 < deg; k0 += 32)
+            {
+                const int k = k0 + lane;
+                const int v = k < deg ? static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask) : 0;
+                int rank = 0;
+                for (int m = 0; m < deg; ++m)
+                {
+                    const int w = static_cast<int>(p.se_col[static_cast<size_t>(m) * stride + i] & kSlotMask);
+                    rank += (w < v) || (w == v && m < k);
+                }
+                if (k < deg)
+                    sh_part[wid][ii][rank] = v;
+            }
+        }
+        __syncwarp();
         for (int dz = -1; dz <= 1; ++dz)
         {
             const int z = cz + dz;
@@ -509,61 +560,145 @@ __global__ void __launch_bounds__(kBuildBlock) k_pairlist(Params p)
                 const int xa = max(cx - 1, 0), xb = min(cx + 1, nx - 1);
                 const int base = (z * ny + y) * nx;
                 const int j0 = p.cell_start[base + xa], j1 = p.cell_start[base + xb + 1];
-                for (int j = j0; j < j1; ++j)
+                for (int jb = j0; jb < j1; jb += 32)
                 {
-                    if (j == s)
-                        continue;
-                    const float4 pj = pos[j];
-                    const float dx = pj.x - pi.x, dy2 = pj.y - pi.y, dz2 = pj.z - pi.z;
-                    const float r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
-                    if (!(r2 < r2max))
-                        continue;
-                    if (deg)
+                    const int j = jb + lane;
+                    const bool jv = j < j1;
+                    const float4 pj = jv ? pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    const unsigned int fj = jv ? fl[j] : 0u;
+                    const bool st = (fj & PF_STATIC) != 0;
+                    for (int ii = 0; ii < nh; ++ii)
                     {
-                        while (nb < static_cast<unsigned int>(j))
-                        {
-                            ++bp;
-                            nb = bp < deg ? (p.se_col[static_cast<size_t>(bp) * stride + s] & kSlotMask) : 0xffffffffu;
-                        }
-                        if (nb == static_cast<unsigned int>(j))
+                        const unsigned int fi = sh_fi[wid][ii];
+                        if (fi & PF_STATIC)
                             continue;
-                    }
-                    const unsigned int fj = fl[j];
-                    const unsigned int entry = static_cast<unsigned int>(j) | ((fj & PF_STATIC) ? kEntryStatic : 0u);
-                    if (on0 && r2 < r2_0)
-                    {
-                        if (cnt0 < cap0)
-                            p.pl[0].idx[static_cast<size_t>(cnt0) * stride + s] = entry;
-                        ++cnt0;
-                    }
-                    if (on1 && (fj & PF_CHARGED) && r2 < r2_1)
-                    {
-                        if (cnt1 < cap1)
-                            p.pl[1].idx[static_cast<size_t>(cnt1) * stride + s] = entry;
-                        ++cnt1;
-                    }
-                    if (on2 && (fj & PF_HYDROPHOBIC) && r2 < r2_2)
-                    {
-                        if (cnt2 < cap2)
-                            p.pl[2].idx[static_cast<size_t>(cnt2) * stride + s] = entry;
-                        ++cnt2;
+                        const int i = hb + ii;
+                        const bool on0 = l0;
+                        const bool on1 = l1 && (fi & PF_CHARGED);
+                        const bool on2 = l2 && (fi & PF_HYDROPHOBIC);
+                        float r2max = on0 ? r2_0 : 0.0f;
+                        if (on1)
+                            r2max = fmaxf(r2max, r2_1);
+                        if (on2)
+                            r2max = fmaxf(r2max, r2_2);
+                        const float4 pi = sh_pi[wid][ii];
+                        const float dx = pj.x - pi.x, dy2 = pj.y - pi.y, dz2 = pj.z - pi.z;
+                        const float r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
+                        bool in = jv && j != i && r2 < r2max;
+                        const int deg = sh_deg[wid][ii];
+                        if (deg > kPlMaxDeg)
+                        {
+                            // many partners: compare with every one of them (global memory)
+                            for (int k = 0; k < deg; ++k)
+                                in = in && static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask) != j;
+                        }
+                        else if (deg > 0)
+                        {
+                            // partners of i inside [jb, jb + 32): the row is sorted, one cursor suffices
+                            const int *part = sh_part[wid][ii];
+                            int bp = sh_bp[wid][ii];
+                            while (bp < deg && part[bp] < jb)
+                                ++bp;
+                            for (int k = bp; k < deg && part[k] < jb + 32; ++k)
+                                in = in && part[k] != j;
+                            __syncwarp();
+                            if (lane == 0)
+                                sh_bp[wid][ii] = bp;
+                        }
+                        if (!__any_sync(0xffffffffu, in))
+                            continue;
+                        if (on0)
+                        {
+                            const bool a0 = in && !st && r2 < r2_0;
+                            const unsigned int m0 = __ballot_sync(0xffffffffu, a0);
+                            const int c0 = sh_cnt[wid][0][ii];
+                            if (a0)
+                            {
+                                const int at = c0 + __popc(m0 & below);
+                                if (at < p.pl[0].cap)
+                                {
+                                    const size_t o = static_cast<size_t>(i) * p.pl[0].cap + at;
+                                    if (PL16)
+                                    {
+                                        const int off = j - i;
+                                        if (off < -32768 || off > 32767)
+                                            atomicOr(&ctl->status, ST_WIDE);
+                                        reinterpret_cast<short *>(p.pl[0].idx)[o] = static_cast<short>(off);
+                                    }
+                                    else
+                                        p.pl[0].idx[o] = static_cast<unsigned int>(j);
+                                }
+                            }
+                            const bool a3 = in && st && r2 < r2_0;
+                            const unsigned int m3 = __ballot_sync(0xffffffffu, a3);
+                            const int c3 = sh_cnt[wid][3][ii];
+                            if (a3)
+                            {
+                                const int at = c3 + __popc(m3 & below);
+                                if (at < p.pl[3].cap)
+                                    p.pl[3].idx[static_cast<size_t>(i) * p.pl[3].cap + at] =
+                                        static_cast<unsigned int>(j) | kEntryStatic;
+                            }
+                            __syncwarp();
+                            if (lane == 0)
+                            {
+                                sh_cnt[wid][0][ii] = c0 + __popc(m0);
+                                sh_cnt[wid][3][ii] = c3 + __popc(m3);
+                            }
+                        }
+                        if (on1)
+                        {
+                            const bool a1 = in && (fj & PF_CHARGED) && r2 < r2_1;
+                            const unsigned int m1 = __ballot_sync(0xffffffffu, a1);
+                            const int c1 = sh_cnt[wid][1][ii];
+                            if (a1)
+                            {
+                                const int at = c1 + __popc(m1 & below);
+                                if (at < p.pl[1].cap)
+                                    p.pl[1].idx[static_cast<size_t>(i) * p.pl[1].cap + at] =
+                                        static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
+                            }
+                            __syncwarp();
+                            if (lane == 0)
+                                sh_cnt[wid][1][ii] = c1 + __popc(m1);
+                        }
+                        if (on2)
+                        {
+                            const bool a2 = in && (fj & PF_HYDROPHOBIC) && r2 < r2_2;
+                            const unsigned int m2 = __ballot_sync(0xffffffffu, a2);
+                            const int c2 = sh_cnt[wid][2][ii];
+                            if (a2)
+                            {
+                                const int at = c2 + __popc(m2 & below);
+                                if (at < p.pl[2].cap)
+                                    p.pl[2].idx[static_cast<size_t>(i) * p.pl[2].cap + at] =
+                                        static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
+                            }
+                            __syncwarp();
+                            if (lane == 0)
+                                sh_cnt[wid][2][ii] = c2 + __popc(m2);
+                        }
+                        __syncwarp();
                     }
                 }
             }
         }
-    }
-    const int cnts[3] = {cnt0, cnt1, cnt2};
-    const int caps[3] = {cap0, cap1, cap2};
-    for (int t = 0; t < kTerms; ++t)
-    {
-        int k = cnts[t];
-        if (k > caps[t])
+        __syncwarp();
+        if (lane < nh)
         {
-            atomicOr(&ctl->status, ST_PAIR_CAPACITY);
-            atomicMax(&ctl->max_row[t], k);
-            k = caps[t];
+            const int i = hb + lane;
+            for (int q = 0; q < kLists; ++q)
+            {
+                int k = sh_cnt[wid][q][lane];
+                if (k > p.pl[q].cap)
+                {
+                    atomicOr(&ctl->status, ST_PAIR_CAPACITY);
+                    atomicMax(&ctl->max_row[q], k);
+                    k = p.pl[q].cap;
+                }
+                p.pl[q].cnt[i] = k;
+            }
         }
-        p.pl[t].cnt[s] = k;
     }
 }
 
@@ -571,14 +706,16 @@ __global__ void __launch_bounds__(kBuildBlock) k_pairlist(Params p)
 // Step kernel
 // ------------------------------------------------------------------------------------------
 
-// Springs of slot s (Spring.cpp:20-34, spring.hpp:17-29). Returns the force before the unit
-// conversion and scale, and the weighted energy before the scale.
-__device__ __forceinline__ void spring_forces(const Params &p, int s, float4 pi, const float4 *__restrict__ pos,
-                                              float &fx, float &fy, float &fz, float &e)
+// Springs of slot s handled by lane t of T (Spring.cpp:20-34, spring.hpp:17-29). Returns the
+// force before the unit conversion and scale, and the weighted energy before the scale.
+template <int T>
+__device__ __forceinline__ void spring_forces(const Params &p, int s, int t, float4 pi,
+                                              const float4 *__restrict__ pos, float &fx, float &fy, float &fz,
+                                              float &e)
 {
     const int deg = p.se_deg[s];
     const size_t stride = static_cast<size_t>(p.npad);
-    for (int k = 0; k < deg; ++k)
+    for (int k = t; k < deg; k += T)
     {
         const size_t at = static_cast<size_t>(k) * stride + s;
         const unsigned int c = __ldg(&p.se_col[at]);
@@ -600,44 +737,54 @@ __device__ __forceinline__ void spring_forces(const Params &p, int s, float4 pi,
     }
 }
 
-// Steric pairs of slot s (Particle.cpp:368-429, steric.hpp:27-156). The loop is
-// software-pipelined: the next entry and its position are loaded before the current pair
-// is evaluated.
-template <int SM>
-__device__ __forceinline__ void steric_forces(const Params &p, int s, float4 pi, float fhi_i,
+// Steric pairs of slot s handled by lane t of T (Particle.cpp:368-429, steric.hpp:27-156).
+// KIND 0: list 0 in 16-bit mode (partner = slot + offset, dynamic partners, half the pair
+// energy); KIND 1: list 0 in 32-bit mode; KIND 2: list 3 (static partners, full energy).
+// The loop is software-pipelined: entries are loaded two iterations ahead of use and
+// positions one iteration ahead.
+template <int SM, int T, int KIND>
+__device__ __forceinline__ void steric_forces(const Params &p, int s, int t, float4 pi, float fhi_i,
                                               const float4 *__restrict__ pos, const float *__restrict__ fhi,
                                               float &fx, float &fy, float &fz, float &e)
 {
-    const PairList &L = p.pl[0];
+    const PairList &L = p.pl[KIND == 2 ? kListStericStatic : 0];
     const int cnt = L.cnt[s];
-    if (cnt <= 0)
+    if (t >= cnt)
         return;
-    const size_t stride = static_cast<size_t>(p.npad);
-    const unsigned int *__restrict__ idx = L.idx + s;
+    const size_t row = static_cast<size_t>(s) * L.cap;
+    const short *__restrict__ idx16 = reinterpret_cast<const short *>(L.idx) + row;
+    const unsigned int *__restrict__ idx32 = L.idx + row;
+    auto entry = [&](int k) -> int {
+        if (KIND == 0)
+            return s + static_cast<int>(__ldg(idx16 + k));
+        return static_cast<int>(__ldg(idx32 + k) & kSlotMask);
+    };
     const float lo2 = p.lo2_s, hi2 = p.hi2_s;
-    unsigned int jn = __ldg(idx);
-    float4 pn = __ldg(&pos[jn & kSlotMask]);
-    for (int k = 0; k < cnt; ++k)
+    const float w = KIND == 2 ? 1.0f : 0.5f;
+    int jn = entry(t);
+    int jn2 = t + T < cnt ? entry(t + T) : 0;
+    float4 pn = __ldg(&pos[jn]);
+    for (int k = t; k < cnt; k += T)
     {
-        const unsigned int j = jn;
+        const int j = jn;
         const float4 pj = pn;
-        if (k + 1 < cnt)
-        {
-            jn = __ldg(idx + static_cast<size_t>(k + 1) * stride);
-            pn = __ldg(&pos[jn & kSlotMask]);
-        }
+        jn = jn2;
+        if (k + 2 * T < cnt)
+            jn2 = entry(k + 2 * T);
+        if (k + T < cnt)
+            pn = __ldg(&pos[jn]);
         const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 >= hi2)
             continue;
         if (!(r2 < lo2 && r2 > 1e-20f) && !exact_pair_test(pi, pj, p.c_steric, false))
             continue;
-        const float w = (j & kEntryStatic) ? 1.0f : 0.5f;
         if (SM == BS_STERIC_LINEAR)
         {
-            // steric.hpp:37-59: E = (d - (ri + rj))^2 / 2 when overlapping, |F| = |d - (ri + rj)|
-            const float inv = r2 > 0.0f ? rsqrt_nr(r2) : 0.0f;
-            const float d = r2 * inv;
+            // steric.hpp:37-59: E = (d - (ri + rj))^2 / 2 when overlapping, |F| = |d - (ri + rj)|.
+            // d - (ri + rj) cancels near contact, so d is the correctly rounded square root here.
+            const float d = sqrtf(r2);
+            const float inv = d > 0.0f ? 1.0f / d : 0.0f;
             const float dv = d - (pi.w + pj.w);
             if (dv > 0.0f)
                 continue;
@@ -654,7 +801,7 @@ __device__ __forceinline__ void steric_forces(const Params &p, int s, float4 pi,
             const float inv2 = recip_nr(r2);
             const float i6 = inv2 * inv2 * inv2;
             const float t6 = pi.w * pj.w * i6;
-            const float hj = __ldg(&fhi[j & kSlotMask]);
+            const float hj = __ldg(&fhi[j]);
             float fod;
             if (SM == BS_STERIC_LJ_12_6_AMBER)
             {
@@ -681,19 +828,20 @@ __device__ __forceinline__ void steric_forces(const Params &p, int s, float4 pi,
     }
 }
 
-// Coulomb pairs of a charged slot (Particle.cpp:191-253, electrostatic.hpp:16-49). With the
-// distance-dependent dielectric eps = D r, E = K q q / (D r^2) and F = -dE/dr.
-__device__ __forceinline__ void coulomb_forces(const Params &p, int s, float4 pi, float qi,
+// Coulomb pairs of a charged slot, lane t of T (Particle.cpp:191-253, electrostatic.hpp:16-49).
+// With the distance-dependent dielectric eps = D r, E = K q q / (D r^2) and F = -dE/dr.
+template <int T>
+__device__ __forceinline__ void coulomb_forces(const Params &p, int s, int t, float4 pi, float qi,
                                                const float4 *__restrict__ pos, const float *__restrict__ chg,
                                                float &fx, float &fy, float &fz, float &e)
 {
     const PairList &L = p.pl[1];
     const int cnt = L.cnt[s];
-    const size_t stride = static_cast<size_t>(p.npad);
+    const unsigned int *__restrict__ row = L.idx + static_cast<size_t>(s) * L.cap;
     const bool dist = p.dielectric_mode == BS_DIELECTRIC_DISTANCE;
-    for (int k = 0; k < cnt; ++k)
+    for (int k = t; k < cnt; k += T)
     {
-        const unsigned int j = __ldg(L.idx + static_cast<size_t>(k) * stride + s);
+        const unsigned int j = __ldg(row + k);
         const float4 pj = __ldg(&pos[j & kSlotMask]);
         const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
@@ -704,33 +852,34 @@ __device__ __forceinline__ void coulomb_forces(const Params &p, int s, float4 pi
         const float inv = rsqrt_nr(r2);
         const float qq = qi * __ldg(&chg[j & kSlotMask]);
         const float w = (j & kEntryStatic) ? 1.0f : 0.5f;
-        float t = qq * inv;
+        float tq = qq * inv;
         float fod;
         if (dist)
         {
-            t *= inv;
-            fod = -2.0f * t * inv * inv;
+            tq *= inv;
+            fod = -2.0f * tq * inv * inv;
         }
         else
-            fod = -t * inv * inv;
-        e = fmaf(w, t, e);
+            fod = -tq * inv * inv;
+        e = fmaf(w, tq, e);
         fx = fmaf(dx, fod, fx);
         fy = fmaf(dy, fod, fy);
         fz = fmaf(dz, fod, fz);
     }
 }
 
-// Hydrophobic pairs (Particle.cpp:269-330, hydrophobic.hpp:20-39).
-__device__ __forceinline__ void hydro_forces(const Params &p, int s, float4 pi, float hi,
+// Hydrophobic pairs, lane t of T (Particle.cpp:269-330, hydrophobic.hpp:20-39).
+template <int T>
+__device__ __forceinline__ void hydro_forces(const Params &p, int s, int t, float4 pi, float hi,
                                              const float4 *__restrict__ pos, const float *__restrict__ hyd,
                                              float &fx, float &fy, float &fz, float &e)
 {
     const PairList &L = p.pl[2];
     const int cnt = L.cnt[s];
-    const size_t stride = static_cast<size_t>(p.npad);
-    for (int k = 0; k < cnt; ++k)
+    const unsigned int *__restrict__ row = L.idx + static_cast<size_t>(s) * L.cap;
+    for (int k = t; k < cnt; k += T)
     {
-        const unsigned int j = __ldg(L.idx + static_cast<size_t>(k) * stride + s);
+        const unsigned int j = __ldg(row + k);
         const float4 pj = __ldg(&pos[j & kSlotMask]);
         const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
@@ -748,7 +897,21 @@ __device__ __forceinline__ void hydro_forces(const Params &p, int s, float4 pi, 
     }
 }
 
-template <int MODE, int SM>
+// Sum over the T consecutive lanes of a particle group (result in every lane of the group).
+template <int T> __device__ __forceinline__ float group_sum(float v)
+{
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// One step (or one force evaluation) for every particle. T consecutive lanes share a particle:
+// each takes every T-th entry of the particle's spring row and pair lists, the group sums its
+// partial forces with shuffles, and the group's first lane adds the per-particle terms and
+// integrates. T > 1 gives the latency-bound gather loops T times more independent loads in
+// flight than one thread per particle would.
+template <int MODE, int SM, int T>
 __global__ void __launch_bounds__(kStepBlock, kStepMinBlocks) k_step(Params p)
 {
     Ctl *ctl = p.ctl;
@@ -756,16 +919,89 @@ __global__ void __launch_bounds__(kStepBlock, kStepMinBlocks) k_step(Params p)
         return;
     const int sb = ctl->sbuf, lb = ctl->lbuf;
     const float4 *__restrict__ pos = p.pos[sb];
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = g / T;
+    const int t = g % T;
+    const bool lead = t == 0;
 
     // energies: spring, steric, coulomb, hydrophobic, imp, kinetic
     float e[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    unsigned int fi = PF_STATIC;
+    float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
     if (s < p.n)
     {
-        const float4 pi = pos[s];
-        const unsigned int fi = p.flags[lb][s];
-        if (fi & PF_STATIC)
+        pi = pos[s];
+        fi = p.flags[lb][s];
+    }
+    const bool active = s < p.n && !(fi & PF_STATIC);
+    if (active)
+    {
+        if (p.spring_on)
+        {
+            float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+            spring_forces<T>(p, s, t, pi, pos, sx, sy, sz, es);
+            const float kf = p.k_spring_f * p.spring_scale;
+            fx = sx * kf;
+            fy = sy * kf;
+            fz = sz * kf;
+            e[0] = es * p.spring_scale;
+        }
+        if (p.steric_on)
+        {
+            float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+            const float fhi_i = p.fhi[lb][s];
+            if (p.pl16)
+                steric_forces<SM, T, 0>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
+            else
+                steric_forces<SM, T, 1>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
+            if (p.pl[kListStericStatic].cnt[s] > 0)
+                steric_forces<SM, T, 2>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
+            const float kf = p.k_spring_f * p.steric_scale;
+            fx = fmaf(sx, kf, fx);
+            fy = fmaf(sy, kf, fy);
+            fz = fmaf(sz, kf, fz);
+            e[1] = es * p.steric_scale;
+        }
+        if (p.coulomb_on && (fi & PF_CHARGED))
+        {
+            float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+            coulomb_forces<T>(p, s, t, pi, p.chg[lb][s], pos, p.chg[lb], sx, sy, sz, es);
+            fx = fmaf(sx, p.k_elec_f, fx);
+            fy = fmaf(sy, p.k_elec_f, fy);
+            fz = fmaf(sz, p.k_elec_f, fz);
+            e[2] = es * p.k_elec_e;
+        }
+        if (p.hydro_on && (fi & PF_HYDROPHOBIC))
+        {
+            float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+            hydro_forces<T>(p, s, t, pi, p.hyd[lb][s], pos, p.hyd[lb], sx, sy, sz, es);
+            const float kf = p.k_spring_f * p.hydro_scale;
+            fx = fmaf(sx, kf, fx);
+            fy = fmaf(sy, kf, fy);
+            fz = fmaf(sz, kf, fz);
+            e[3] = es * p.k_hydro_e * p.hydro_scale;
+        }
+    }
+    if (T > 1)
+    {
+        // every lane of the warp takes part in the group reductions
+        fx = group_sum<T>(fx);
+        fy = group_sum<T>(fy);
+        fz = group_sum<T>(fz);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            e[k] = group_sum<T>(e[k]);
+        if (!lead)
+        {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                e[k] = 0.f;
+        }
+    }
+    if (lead && s < p.n)
+    {
+        if (!active)
         {
             if (MODE == MODE_STEP)
             {
@@ -777,46 +1013,6 @@ __global__ void __launch_bounds__(kStepBlock, kStepMinBlocks) k_step(Params p)
         }
         else
         {
-            float fx = 0.f, fy = 0.f, fz = 0.f;
-            if (p.spring_on)
-            {
-                float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
-                spring_forces(p, s, pi, pos, sx, sy, sz, es);
-                const float kf = p.k_spring_f * p.spring_scale;
-                fx = sx * kf;
-                fy = sy * kf;
-                fz = sz * kf;
-                e[0] = es * p.spring_scale;
-            }
-            if (p.steric_on)
-            {
-                float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
-                steric_forces<SM>(p, s, pi, p.fhi[lb][s], pos, p.fhi[lb], sx, sy, sz, es);
-                const float kf = p.k_spring_f * p.steric_scale;
-                fx = fmaf(sx, kf, fx);
-                fy = fmaf(sy, kf, fy);
-                fz = fmaf(sz, kf, fz);
-                e[1] = es * p.steric_scale;
-            }
-            if (p.coulomb_on && (fi & PF_CHARGED))
-            {
-                float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
-                coulomb_forces(p, s, pi, p.chg[lb][s], pos, p.chg[lb], sx, sy, sz, es);
-                fx = fmaf(sx, p.k_elec_f, fx);
-                fy = fmaf(sy, p.k_elec_f, fy);
-                fz = fmaf(sz, p.k_elec_f, fz);
-                e[2] = es * p.k_elec_e;
-            }
-            if (p.hydro_on && (fi & PF_HYDROPHOBIC))
-            {
-                float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
-                hydro_forces(p, s, pi, p.hyd[lb][s], pos, p.hyd[lb], sx, sy, sz, es);
-                const float kf = p.k_spring_f * p.hydro_scale;
-                fx = fmaf(sx, kf, fx);
-                fy = fmaf(sy, kf, fy);
-                fz = fmaf(sz, kf, fz);
-                e[3] = es * p.k_hydro_e * p.hydro_scale;
-            }
             const float4 v = p.vel[sb][s];
             // ---- viscosity (Particle.cpp:80-84) ----
             if (p.visc_on)
@@ -831,15 +1027,15 @@ __global__ void __launch_bounds__(kStepBlock, kStepMinBlocks) k_step(Params p)
             {
                 const float ex = expf(p.imp_alpha * (fabsf(pi.z) - p.imp_z0));
                 const float cz = 0.5f - 1.0f / (1.0f + ex);
-                const float g = -ip.y * ip.z + kAlip * ip.y;
-                e[4] = p.imp_scale * g * cz;
+                const float gg = -ip.y * ip.z + kAlip * ip.y;
+                e[4] = p.imp_scale * gg * cz;
                 // dC/dz = alpha sign(z) e / (1 + e)^2, written without overflow
                 float dcz = pi.z != 0.0f ? p.imp_alpha / (ex + 2.0f + 1.0f / ex) : 0.0f;
                 if (pi.z < 0.0f)
                     dcz = -dcz;
                 if (!isfinite(dcz))
                     dcz = 0.0f;
-                fz -= p.imp_scale * (g * dcz * p.k_imp_f);
+                fz -= p.imp_scale * (gg * dcz * p.k_imp_f);
             }
             // ---- external force (SpringNetwork::setForce, SpringNetwork.cpp:438-442) ----
             if (ctl->ext_pending)
@@ -1039,12 +1235,10 @@ __global__ void __launch_bounds__(kStepBlock) k_diag_pairs(Params p, int term, l
     const unsigned int fi = p.flags[ctl->lbuf][s];
     if (fi & PF_STATIC)
         return;
-    const PairList &L = p.pl[term];
-    if (!L.on)
+    if (!p.pl[term].on)
         return;
     const float4 pi = pos[s];
     const int idi = p.perm[ctl->lbuf][s];
-    const int cnt = L.cnt[s];
     float lo2 = p.lo2_s, hi2 = p.hi2_s, cut = p.c_steric;
     if (term == BS_TERM_COULOMB)
     {
@@ -1058,13 +1252,27 @@ __global__ void __launch_bounds__(kStepBlock) k_diag_pairs(Params p, int term, l
         hi2 = p.hi2_h;
         cut = p.c_hydro;
     }
+    // the steric term has two lists: dynamic partners (0) and static partners (3)
+    for (int pass = 0; pass < 2; ++pass)
+    {
+    const int li = pass == 0 ? term : kListStericStatic;
+    if (pass == 1 && term != BS_TERM_STERIC)
+        break;
+    const PairList &L = p.pl[li];
+    const int cnt = L.cnt[s];
     for (int k = 0; k < cnt; ++k)
     {
-        const unsigned int e = L.idx[static_cast<size_t>(k) * p.npad + s];
+        unsigned int e;
+        const size_t pos_in_row = static_cast<size_t>(s) * L.cap + k;
+        if (li == 0 && p.pl16)
+            e = static_cast<unsigned int>(s + reinterpret_cast<const short *>(L.idx)[pos_in_row]);
+        else
+            e = L.idx[pos_in_row];
         const int j = static_cast<int>(e & kSlotMask);
         const float4 pj = pos[j];
         const int idj = p.perm[ctl->lbuf][j];
-        if (!(e & kEntryStatic) && idj < idi)
+        const bool j_static = (p.flags[ctl->lbuf][j] & PF_STATIC) != 0;
+        if (!j_static && idj < idi)
             continue;
         const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
@@ -1076,6 +1284,7 @@ __global__ void __launch_bounds__(kStepBlock) k_diag_pairs(Params p, int term, l
             out[2 * at] = min(idi, idj);
             out[2 * at + 1] = max(idi, idj);
         }
+    }
     }
 }
 
@@ -1094,19 +1303,46 @@ int launch_rebuild(const Params &p, cudaStream_t st)
     k_cell_sort<<<1216, kBuildBlock, 0, st>>>(p);
     k_reorder<<<nb, kBuildBlock, 0, st>>>(p);
     k_spring_ell<<<nbp, kBuildBlock, 0, st>>>(p);
-    k_pairlist<<<nbp, kBuildBlock, 0, st>>>(p);
+    // kPlBatchesPerCell warps per cell of the grid (its size is only known on the device: cover
+    // the capacity; warps past the last cell return at once)
+    const int plb = static_cast<int>((static_cast<long long>(p.cell_cap) * kPlBatchesPerCell + kPlWarps - 1) / kPlWarps);
+    if (p.pl16)
+        k_pairlist<true><<<plb, kPlWarps * 32, 0, st>>>(p);
+    else
+        k_pairlist<false><<<plb, kPlWarps * 32, 0, st>>>(p);
     return 8;
+}
+
+template <int MODE, int SM>
+static void launch_step_lanes(const Params &p, cudaStream_t st)
+{
+    const long long threads_per = p.step_lanes;
+    const int nb = static_cast<int>((static_cast<long long>(p.n) * threads_per + kStepBlock - 1) / kStepBlock);
+    switch (p.step_lanes)
+    {
+    case 1:
+        k_step<MODE, SM, 1><<<nb, kStepBlock, 0, st>>>(p);
+        break;
+    case 2:
+        k_step<MODE, SM, 2><<<nb, kStepBlock, 0, st>>>(p);
+        break;
+    case 8:
+        k_step<MODE, SM, 8><<<nb, kStepBlock, 0, st>>>(p);
+        break;
+    default:
+        k_step<MODE, SM, 4><<<nb, kStepBlock, 0, st>>>(p);
+        break;
+    }
 }
 
 int launch_step(const Params &p, int mode, cudaStream_t st)
 {
-    const int nb = (p.n + kStepBlock - 1) / kStepBlock;
 #define BS_STEP_CASE(SMV)                                                                                              \
     case SMV:                                                                                                          \
         if (mode == MODE_STEP)                                                                                         \
-            k_step<MODE_STEP, SMV><<<nb, kStepBlock, 0, st>>>(p);                                                      \
+            launch_step_lanes<MODE_STEP, SMV>(p, st);                                                                  \
         else                                                                                                           \
-            k_step<MODE_FORCES, SMV><<<nb, kStepBlock, 0, st>>>(p);                                                    \
+            launch_step_lanes<MODE_FORCES, SMV>(p, st);                                                                \
         break;
     switch (p.steric_mode)
     {

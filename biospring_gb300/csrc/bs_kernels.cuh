@@ -13,11 +13,16 @@ constexpr int kStepBlock = 128;
 // resident blocks of 128 threads per SM the step kernel is compiled for (8: at most 64 registers)
 constexpr int kStepMinBlocks = BS_STEP_MIN_BLOCKS;
 constexpr int kBuildBlock = 128;
+constexpr int kBuildLanes = 8;    // lanes sharing one particle in the pair-list build
 constexpr int kBboxBlock = 256;
 constexpr int kMaxEnergyBlocks = 1 << 16;
 
 // status bits that stop a rebuild; a stale list is what a rebuild repairs
-constexpr int kRebuildBlocking = ST_NONFINITE | ST_PAIR_CAPACITY | ST_CELL_CAPACITY;
+constexpr int kRebuildBlocking = ST_NONFINITE | ST_PAIR_CAPACITY | ST_CELL_CAPACITY | ST_WIDE;
+constexpr int kPlWarps = 4;          // warps per block in the pair-list build
+constexpr int kPlBatch = 16;         // home particles per warp
+constexpr int kPlBatchesPerCell = 4; // warps per cell (a cell with more than 64 particles loops)
+constexpr int kPlMaxDeg = 48;        // spring partners kept in shared memory per home particle
 
 enum StepMode
 {

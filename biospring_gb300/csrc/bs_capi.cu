@@ -668,7 +668,7 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     double cells = 1.0, volume = 1.0;
     for (int k = 0; k < 3; ++k)
     {
-        cells *= std::ceil((hi[k] - lo[k]) / list_radius) + 3.0;
+        cells *= std::ceil((hi[k] - lo[k]) / (list_radius / kGridDiv)) + 3.0;
         volume *= std::max(hi[k] - lo[k], 1.0);
     }
     const int cell_cap = static_cast<int>(std::min(2.0 * cells + 1024.0, 2.0e8));

@@ -24,7 +24,9 @@
 // on forces, so results are deterministic) and integrates in the same pass.
 //
 // Reference behaviour reproduced (paths inside the BioSpring project):
-//   cell grid and cell id           src/nsearch.hpp:277-293, 342-390 (FP64, same formula)
+//   cell grid and cell id           src/nsearch.hpp:277-293, 342-390 (FP64, same formula; the
+//                                   search grid uses edge (cutoff + skin) / kGridDiv, the
+//                                   diagnostic grid of bs_get_cells the reference edge)
 //   pair filters                    src/nsearch.hpp:230 (FP64 distance) and src/spn/Particle.cpp:
 //                                   213-224 (spring exclusion, float distance < cutoff, != 0),
 //                                   :209 (static neighbour: full energy, no force on it)
@@ -277,7 +279,8 @@ __global__ void __launch_bounds__(kBboxBlock) k_bbox(Params p)
         enc[3 + k] = 0u;
     }
     // Grid dimensions, reference formula ncells = ceil(len / radius) + 1 (nsearch.hpp:351-354).
-    const double r = static_cast<double>(p.list_radius);
+    const float edge = p.list_radius / static_cast<float>(kGridDiv);
+    const double r = static_cast<double>(edge);
     double cells = 1.0;
     int nc[3];
     for (int k = 0; k < 3; ++k)
@@ -288,7 +291,7 @@ __global__ void __launch_bounds__(kBboxBlock) k_bbox(Params p)
         nc[k] = c < 1.0e9 ? static_cast<int>(c) : 1000000000;
         ctl->gmin[k] = static_cast<double>(mn[k]);
     }
-    ctl->gradius = p.list_radius;
+    ctl->gradius = edge;
     ctl->gnx = nc[0];
     ctl->gny = nc[1];
     ctl->gnz = nc[2];
@@ -467,229 +470,218 @@ __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
 // static partners apart), Coulomb (both charged) and hydrophobic (both hydrophobic), minus the
 // slot itself and, when springs are enabled, its spring partners (Particle.cpp:213-218).
 //
-// A warp owns a batch of up to kPlBatch home particles of one cell. The candidates of the 27
-// neighbouring cells form nine contiguous x-runs of slots; each run is taken 32 slots at a time,
-// one candidate per lane (coalesced loads). For every home particle of the batch, in turn, the
-// lanes test their candidates, the warp ballots the accepted ones and appends them to the home
-// particle's row-major row at consecutive positions (coalesced stores). Control flow depends
-// only on the home particle, so lanes never diverge; rows come out in ascending slot order.
-// Bonded partners are excluded with the home particle's sorted spring row: only the partners
-// falling in the current 32-slot window are compared. In 16-bit mode the steric row holds
-// partner-minus-slot offsets.
+// A block owns one cell and its kPlWarps warps share the cell's home particles (warp w takes
+// every kPlWarps-th one). The grid edge is (cutoff + skin) / kGridDiv, so the neighbourhood is a
+// (2 kGridDiv + 1)^3 block of cells, i.e. (2 kGridDiv + 1)^2 contiguous x-runs of slots, staged
+// in shared memory. For one home particle at a time a warp walks the runs, 32 candidates per pass, one per lane
+// (coalesced loads; the block's warps read the same runs, so they mostly hit L1). Accepted
+// candidates are found with one ballot and appended to the home particle's row-major row at
+// consecutive positions (coalesced stores); the home particle's state stays in registers and
+// lanes never diverge. Rows come out in ascending slot order. Bonded partners are excluded with
+// the home particle's spring partners, sorted in shared memory, of which only those inside the
+// current 32-slot window are compared. In 16-bit mode the steric row holds partner-minus-slot
+// offsets.
 template <bool PL16>
 __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
 {
-    constexpr int HB = kPlBatch;
-    __shared__ float4 sh_pi[kPlWarps][HB];
-    __shared__ unsigned int sh_fi[kPlWarps][HB];
-    __shared__ int sh_bp[kPlWarps][HB];
-    __shared__ int sh_deg[kPlWarps][HB];
-    __shared__ int sh_cnt[kPlWarps][kLists][HB];
-    __shared__ int sh_part[kPlWarps][HB][kPlMaxDeg]; // sorted spring partners of the batch
-    __shared__ int blocked;
+    __shared__ int sh_part[kPlWarps][kPlMaxDeg];
+    __shared__ int sh_raw[kPlWarps][kPlMaxDeg];
+    constexpr int kRuns = (2 * kGridDiv + 1) * (2 * kGridDiv + 1);
+    __shared__ int sh_run[kRuns][3]; // first slot, end slot, offset in the stage
+    __shared__ float4 sh_pos[kPlStage];
+    __shared__ int blocked, staged;
     Ctl *ctl = p.ctl;
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nx = ctl->gnx, ny = ctl->gny, nz = ctl->gnz;
+    const int c = blockIdx.x;
     if (threadIdx.x == 0)
-        blocked = status_of(ctl) & kRebuildBlocking;
+        blocked = (status_of(ctl) & kRebuildBlocking) || c >= nx * ny * nz;
     __syncthreads();
     if (blocked)
         return;
-    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nx = ctl->gnx, ny = ctl->gny, nz = ctl->gnz;
-    const int gw = blockIdx.x * kPlWarps + wid;
-    const int c = gw / kPlBatchesPerCell;
-    const int b0 = gw % kPlBatchesPerCell;
-    if (c >= nx * ny * nz)
-        return;
     const int h0 = p.cell_start[c], h1 = p.cell_start[c + 1];
-    if (h0 + b0 * HB >= h1)
+    if (h0 == h1)
         return;
+    const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
+    if (threadIdx.x < kRuns)
+    {
+        constexpr int w = 2 * kGridDiv + 1;
+        const int y = cy + static_cast<int>(threadIdx.x % w) - kGridDiv;
+        const int z = cz + static_cast<int>(threadIdx.x / w) - kGridDiv;
+        int j0 = 0, j1 = 0;
+        if (y >= 0 && y < ny && z >= 0 && z < nz)
+        {
+            const int base = (z * ny + y) * nx;
+            j0 = p.cell_start[base + max(cx - kGridDiv, 0)];
+            j1 = p.cell_start[base + min(cx + kGridDiv, nx - 1) + 1];
+        }
+        sh_run[threadIdx.x][0] = j0;
+        sh_run[threadIdx.x][1] = j1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        int tot = 0, lo = h0, hi = h1;
+        for (int r = 0; r < kRuns; ++r)
+        {
+            sh_run[r][2] = tot;
+            const int len = sh_run[r][1] - sh_run[r][0];
+            tot += len;
+            if (len > 0)
+            {
+                lo = min(lo, sh_run[r][0]);
+                hi = max(hi, sh_run[r][1]);
+            }
+        }
+        staged = tot <= kPlStage;
+        // every candidate offset of this cell fits 16 bits, or the list goes 32-bit
+        if (PL16 && (hi - 1 - h0 > 32767 || lo - (h1 - 1) < -32768))
+            atomicOr(&ctl->status, ST_WIDE);
+    }
+    __syncthreads();
+    // the candidate positions of the 27 cells are read by every warp of the block: stage them
+    if (staged)
+        for (int r = 0; r < kRuns; ++r)
+        {
+            const int j0 = sh_run[r][0], len = sh_run[r][1] - j0, o = sh_run[r][2];
+            for (int k = threadIdx.x; k < len; k += blockDim.x)
+                sh_pos[o + k] = p.pos[ctl->sbuf][j0 + k];
+        }
+    __syncthreads();
     const int sb = ctl->sbuf, lb = ctl->lbuf;
     const float4 *__restrict__ pos = p.pos[sb];
     const unsigned int *__restrict__ fl = p.flags[lb];
-    const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
     const float r2_0 = p.pl[0].r2, r2_1 = p.pl[1].r2, r2_2 = p.pl[2].r2;
-    const bool l0 = p.pl[0].on, l1 = p.pl[1].on, l2 = p.pl[2].on;
+    const bool l0 = p.pl[0].on, l1 = p.pl[1].on, l2 = p.pl[2].on, l3 = p.pl[3].on;
+    const int cap0 = p.pl[0].cap, cap1 = p.pl[1].cap, cap2 = p.pl[2].cap, cap3 = p.pl[3].cap;
     const size_t stride = static_cast<size_t>(p.npad);
     const unsigned int below = (1u << lane) - 1u;
-    for (int hb = h0 + b0 * HB; hb < h1; hb += HB * kPlBatchesPerCell)
+    int *part = sh_part[wid];
+    for (int i = h0 + wid; i < h1; i += kPlWarps)
     {
-        const int nh = min(HB, h1 - hb);
-        __syncwarp();
-        if (lane < nh)
+        const unsigned int fi = fl[i];
+        const bool dyn = !(fi & PF_STATIC);
+        const bool on0 = dyn && l0;
+        const bool on1 = dyn && l1 && (fi & PF_CHARGED);
+        const bool on2 = dyn && l2 && (fi & PF_HYDROPHOBIC);
+        const bool need_fj = l3 || on1 || on2;
+        float r2max = on0 ? r2_0 : 0.0f;
+        if (on1)
+            r2max = fmaxf(r2max, r2_1);
+        if (on2)
+            r2max = fmaxf(r2max, r2_2);
+        int cnt0 = 0, cnt1 = 0, cnt2 = 0, cnt3 = 0;
+        if (on0 || on1 || on2)
         {
-            sh_pi[wid][lane] = pos[hb + lane];
-            sh_fi[wid][lane] = fl[hb + lane];
-            sh_bp[wid][lane] = 0;
-            sh_deg[wid][lane] = p.spring_on ? p.se_deg[hb + lane] : 0;
-            for (int q = 0; q < kLists; ++q)
-                sh_cnt[wid][q][lane] = 0;
-        }
-        __syncwarp();
-        // spring partners of each home particle, sorted ascending (rank sort across the warp)
-        for (int ii = 0; ii < nh; ++ii)
-        {
-            const int deg = sh_deg[wid][ii];
-            if (deg > kPlMaxDeg)
-                continue; // scanned from global memory below
-            const int i = hb + ii;
-            for (int k0 = 0; k0 < deg; k0 += 32)
+            const float4 pi = pos[i];
+            // spring partners of i, sorted ascending in shared memory (rank sort across the warp)
+            const int deg = p.spring_on ? p.se_deg[i] : 0;
+            const bool small = deg <= kPlMaxDeg;
+            __syncwarp();
+            if (small)
             {
-                const int k = k0 + lane;
-                const int v = k < deg ? static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask) : 0;
-                int rank = 0;
-                for (int m = 0; m < deg; ++m)
+                int *raw = sh_raw[wid];
+                for (int k = lane; k < deg; k += 32)
+                    raw[k] = static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask);
+                __syncwarp();
+                for (int k = lane; k < deg; k += 32)
                 {
-                    const int w = static_cast<int>(p.se_col[static_cast<size_t>(m) * stride + i] & kSlotMask);
-                    rank += (w < v) || (w == v && m < k);
+                    const int v = raw[k];
+                    int rank = 0;
+                    for (int m = 0; m < deg; ++m)
+                    {
+                        const int w = raw[m];
+                        rank += (w < v) || (w == v && m < k);
+                    }
+                    part[rank] = v;
                 }
-                if (k < deg)
-                    sh_part[wid][ii][rank] = v;
             }
-        }
-        __syncwarp();
-        for (int dz = -1; dz <= 1; ++dz)
-        {
-            const int z = cz + dz;
-            if (z < 0 || z >= nz)
-                continue;
-            for (int dy = -1; dy <= 1; ++dy)
+            __syncwarp();
+            int bp = 0;
+            short *row0s = reinterpret_cast<short *>(p.pl[0].idx) + static_cast<size_t>(i) * cap0;
+            unsigned int *row0 = p.pl[0].idx + static_cast<size_t>(i) * cap0;
+            unsigned int *row1 = p.pl[1].idx + static_cast<size_t>(i) * cap1;
+            unsigned int *row2 = p.pl[2].idx + static_cast<size_t>(i) * cap2;
+            unsigned int *row3 = p.pl[3].idx + static_cast<size_t>(i) * cap3;
+            for (int r = 0; r < kRuns; ++r)
             {
-                const int y = cy + dy;
-                if (y < 0 || y >= ny)
-                    continue;
-                const int xa = max(cx - 1, 0), xb = min(cx + 1, nx - 1);
-                const int base = (z * ny + y) * nx;
-                const int j0 = p.cell_start[base + xa], j1 = p.cell_start[base + xb + 1];
+                const int j0 = sh_run[r][0], j1 = sh_run[r][1];
+                const float4 *src = staged ? sh_pos + sh_run[r][2] - j0 : pos;
                 for (int jb = j0; jb < j1; jb += 32)
                 {
                     const int j = jb + lane;
                     const bool jv = j < j1;
-                    const float4 pj = jv ? pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-                    const unsigned int fj = jv ? fl[j] : 0u;
-                    const bool st = (fj & PF_STATIC) != 0;
-                    for (int ii = 0; ii < nh; ++ii)
+                    const int jc = jv ? j : j1 - 1;
+                    const float4 pj = src[jc];
+                    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    bool in = jv && r2 < r2max && j != i;
+                    if (deg)
                     {
-                        const unsigned int fi = sh_fi[wid][ii];
-                        if (fi & PF_STATIC)
-                            continue;
-                        const int i = hb + ii;
-                        const bool on0 = l0;
-                        const bool on1 = l1 && (fi & PF_CHARGED);
-                        const bool on2 = l2 && (fi & PF_HYDROPHOBIC);
-                        float r2max = on0 ? r2_0 : 0.0f;
-                        if (on1)
-                            r2max = fmaxf(r2max, r2_1);
-                        if (on2)
-                            r2max = fmaxf(r2max, r2_2);
-                        const float4 pi = sh_pi[wid][ii];
-                        const float dx = pj.x - pi.x, dy2 = pj.y - pi.y, dz2 = pj.z - pi.z;
-                        const float r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
-                        bool in = jv && j != i && r2 < r2max;
-                        const int deg = sh_deg[wid][ii];
-                        if (deg > kPlMaxDeg)
+                        if (small)
                         {
-                            // many partners: compare with every one of them (global memory)
-                            for (int k = 0; k < deg; ++k)
-                                in = in && static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask) != j;
-                        }
-                        else if (deg > 0)
-                        {
-                            // partners of i inside [jb, jb + 32): the row is sorted, one cursor suffices
-                            const int *part = sh_part[wid][ii];
-                            int bp = sh_bp[wid][ii];
                             while (bp < deg && part[bp] < jb)
                                 ++bp;
                             for (int k = bp; k < deg && part[k] < jb + 32; ++k)
                                 in = in && part[k] != j;
-                            __syncwarp();
-                            if (lane == 0)
-                                sh_bp[wid][ii] = bp;
                         }
-                        if (!__any_sync(0xffffffffu, in))
-                            continue;
-                        if (on0)
+                        else
+                            for (int k = 0; k < deg; ++k)
+                                in = in && static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask) != j;
+                    }
+                    const unsigned int fj = need_fj ? fl[jc] : 0u;
+                    const bool st = (fj & PF_STATIC) != 0;
+                    if (on0)
+                    {
+                        const bool a0 = in && !st && r2 < r2_0;
+                        const unsigned int m0 = __ballot_sync(0xffffffffu, a0);
+                        if (a0)
                         {
-                            const bool a0 = in && !st && r2 < r2_0;
-                            const unsigned int m0 = __ballot_sync(0xffffffffu, a0);
-                            const int c0 = sh_cnt[wid][0][ii];
-                            if (a0)
+                            const int at = cnt0 + __popc(m0 & below);
+                            if (at < cap0)
                             {
-                                const int at = c0 + __popc(m0 & below);
-                                if (at < p.pl[0].cap)
-                                {
-                                    const size_t o = static_cast<size_t>(i) * p.pl[0].cap + at;
-                                    if (PL16)
-                                    {
-                                        const int off = j - i;
-                                        if (off < -32768 || off > 32767)
-                                            atomicOr(&ctl->status, ST_WIDE);
-                                        reinterpret_cast<short *>(p.pl[0].idx)[o] = static_cast<short>(off);
-                                    }
-                                    else
-                                        p.pl[0].idx[o] = static_cast<unsigned int>(j);
-                                }
+                                if (PL16)
+                                    row0s[at] = static_cast<short>(j - i);
+                                else
+                                    row0[at] = static_cast<unsigned int>(j);
                             }
+                        }
+                        cnt0 += __popc(m0);
+                        if (l3)
+                        {
                             const bool a3 = in && st && r2 < r2_0;
                             const unsigned int m3 = __ballot_sync(0xffffffffu, a3);
-                            const int c3 = sh_cnt[wid][3][ii];
-                            if (a3)
-                            {
-                                const int at = c3 + __popc(m3 & below);
-                                if (at < p.pl[3].cap)
-                                    p.pl[3].idx[static_cast<size_t>(i) * p.pl[3].cap + at] =
-                                        static_cast<unsigned int>(j) | kEntryStatic;
-                            }
-                            __syncwarp();
-                            if (lane == 0)
-                            {
-                                sh_cnt[wid][0][ii] = c0 + __popc(m0);
-                                sh_cnt[wid][3][ii] = c3 + __popc(m3);
-                            }
+                            if (a3 && cnt3 + __popc(m3 & below) < cap3)
+                                row3[cnt3 + __popc(m3 & below)] = static_cast<unsigned int>(j) | kEntryStatic;
+                            cnt3 += __popc(m3);
                         }
-                        if (on1)
-                        {
-                            const bool a1 = in && (fj & PF_CHARGED) && r2 < r2_1;
-                            const unsigned int m1 = __ballot_sync(0xffffffffu, a1);
-                            const int c1 = sh_cnt[wid][1][ii];
-                            if (a1)
-                            {
-                                const int at = c1 + __popc(m1 & below);
-                                if (at < p.pl[1].cap)
-                                    p.pl[1].idx[static_cast<size_t>(i) * p.pl[1].cap + at] =
-                                        static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
-                            }
-                            __syncwarp();
-                            if (lane == 0)
-                                sh_cnt[wid][1][ii] = c1 + __popc(m1);
-                        }
-                        if (on2)
-                        {
-                            const bool a2 = in && (fj & PF_HYDROPHOBIC) && r2 < r2_2;
-                            const unsigned int m2 = __ballot_sync(0xffffffffu, a2);
-                            const int c2 = sh_cnt[wid][2][ii];
-                            if (a2)
-                            {
-                                const int at = c2 + __popc(m2 & below);
-                                if (at < p.pl[2].cap)
-                                    p.pl[2].idx[static_cast<size_t>(i) * p.pl[2].cap + at] =
-                                        static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
-                            }
-                            __syncwarp();
-                            if (lane == 0)
-                                sh_cnt[wid][2][ii] = c2 + __popc(m2);
-                        }
-                        __syncwarp();
+                    }
+                    if (on1)
+                    {
+                        const bool a1 = in && (fj & PF_CHARGED) && r2 < r2_1;
+                        const unsigned int m1 = __ballot_sync(0xffffffffu, a1);
+                        if (a1 && cnt1 + __popc(m1 & below) < cap1)
+                            row1[cnt1 + __popc(m1 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
+                        cnt1 += __popc(m1);
+                    }
+                    if (on2)
+                    {
+                        const bool a2 = in && (fj & PF_HYDROPHOBIC) && r2 < r2_2;
+                        const unsigned int m2 = __ballot_sync(0xffffffffu, a2);
+                        if (a2 && cnt2 + __popc(m2 & below) < cap2)
+                            row2[cnt2 + __popc(m2 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
+                        cnt2 += __popc(m2);
                     }
                 }
             }
         }
-        __syncwarp();
-        if (lane < nh)
+        if (lane == 0)
         {
-            const int i = hb + lane;
+            const int cnts[kLists] = {cnt0, cnt1, cnt2, cnt3};
+#pragma unroll
             for (int q = 0; q < kLists; ++q)
             {
-                int k = sh_cnt[wid][q][lane];
+                int k = cnts[q];
                 if (k > p.pl[q].cap)
                 {
                     atomicOr(&ctl->status, ST_PAIR_CAPACITY);
@@ -1303,9 +1295,9 @@ int launch_rebuild(const Params &p, cudaStream_t st)
     k_cell_sort<<<1216, kBuildBlock, 0, st>>>(p);
     k_reorder<<<nb, kBuildBlock, 0, st>>>(p);
     k_spring_ell<<<nbp, kBuildBlock, 0, st>>>(p);
-    // kPlBatchesPerCell warps per cell of the grid (its size is only known on the device: cover
-    // the capacity; warps past the last cell return at once)
-    const int plb = static_cast<int>((static_cast<long long>(p.cell_cap) * kPlBatchesPerCell + kPlWarps - 1) / kPlWarps);
+    // one block per cell of the grid (its size is only known on the device: cover the capacity;
+    // blocks past the last cell return at once)
+    const int plb = p.cell_cap;
     if (p.pl16)
         k_pairlist<true><<<plb, kPlWarps * 32, 0, st>>>(p);
     else

@@ -19,7 +19,18 @@ constexpr int kMaxEnergyBlocks = 1 << 16;
 
 // status bits that stop a rebuild; a stale list is what a rebuild repairs
 constexpr int kRebuildBlocking = ST_NONFINITE | ST_PAIR_CAPACITY | ST_CELL_CAPACITY | ST_WIDE;
-constexpr int kPlWarps = 4;          // warps per block in the pair-list build
+#ifndef BS_GRID_DIV
+#define BS_GRID_DIV 1
+#endif
+#ifndef BS_PL_WARPS
+#define BS_PL_WARPS 8
+#endif
+#ifndef BS_PL_STAGE
+#define BS_PL_STAGE 2048
+#endif
+constexpr int kGridDiv = BS_GRID_DIV; // search-grid cells per list radius (stencil of +-kGridDiv cells)
+constexpr int kPlWarps = BS_PL_WARPS; // warps per block (one cell) in the pair-list build
+constexpr int kPlStage = BS_PL_STAGE; // candidate positions staged in shared memory per block
 constexpr int kPlBatch = 16;         // home particles per warp
 constexpr int kPlBatchesPerCell = 4; // warps per cell (a cell with more than 64 particles loops)
 constexpr int kPlMaxDeg = 48;        // spring partners kept in shared memory per home particle

@@ -223,6 +223,35 @@ int bs_get_launch_count(bs_sim *sim, int64_t *count);
 /* Copies the last error message of the handle (or of the library when sim is NULL). */
 int bs_last_error(bs_sim *sim, char *buf, size_t len);
 
+/* ---- nonbonded forces without allocation (no counterpart in the reference) ------
+ *
+ * Steric, Coulomb and hydrophobic forces and energies of at most
+ * BS_NOALLOC_MAX_PARTICLES particles by direct summation over all pairs. Unlike the
+ * rest of this API it takes DEVICE pointers the caller owns and allocates no memory:
+ * its scratch is a fixed array inside the library. It is for callers whose device
+ * memory is all managed by their own pool, or that evaluate forces inside a frame
+ * budget where an allocation could stall or fail.
+ *
+ * Same pair rules as the handle's force evaluation with spring.enable = 0 (no pair is
+ * excluded); spring, IMPALA, viscosity and rigid-body fields of *cfg are ignored.
+ * d_radius is required when steric is on, d_epsilon too in the Lennard-Jones modes;
+ * d_charge, d_hydrophobicity and d_is_static may be NULL (no charges, no hydrophobic
+ * particles, all dynamic). Outputs: d_forces float[3n] (0 for static particles),
+ * d_energies double[BS_NUM_ENERGIES] (steric, electrostatic and hydrophobic filled,
+ * the rest 0). Asynchronous on `stream` (a cudaStream_t, NULL = default stream).
+ *
+ * n outside [1, BS_NOALLOC_MAX_PARTICLES] returns BS_E_ARG. The first call on a device
+ * sets up the scratch (it loads the kernels onto that device) and should come before
+ * any stream capture. All calls on one device share the scratch: two calls in flight
+ * at once (other streams, other threads) race; order them on one stream. err
+ * (nullable) receives a one-line message on failure. */
+#define BS_NOALLOC_MAX_PARTICLES 16384
+int bs_nonbonded_forces_noalloc(const bs_config *cfg, int64_t n, const float *d_xyz,
+                                const float *d_radius, const float *d_epsilon,
+                                const float *d_charge, const float *d_hydrophobicity,
+                                const uint8_t *d_is_static, float *d_forces, double *d_energies,
+                                void *stream, char *err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -115,6 +115,11 @@ SIGNATURES = {
     "bs_get_cells": (C.c_int, [C.c_void_p, C.c_int32, _i64p]),
     "bs_get_launch_count": (C.c_int, [C.c_void_p, _i64p]),
     "bs_last_error": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+    "bs_set_systems": (C.c_int, [C.c_void_p, C.c_int32, _i64p]),
+    "bs_get_system_energies": (C.c_int, [C.c_void_p, _f64p]),
+    "bs_set_batch_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "bs_get_batch_shape": (C.c_int, [C.c_void_p, _i32p]),
+    "bs_batch_autotune": (C.c_int, [C.c_void_p, _i32p]),
 }
 
 _lib = None

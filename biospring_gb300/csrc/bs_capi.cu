@@ -78,6 +78,11 @@ struct bs_sim
     // growable buffers (pair lists, grid arrays), freed on regrowth
     unsigned int *pl_idx[kLists] = {nullptr, nullptr, nullptr, nullptr};
     int *cell_buf[3] = {nullptr, nullptr, nullptr};
+    // batched ensembles: caller's partition into systems (empty: one system)
+    std::vector<int64_t> sys_off;
+    BatchShape shape{256, 4, 1};
+    int *cl_start_d = nullptr;
+    int *cl_sys_d = nullptr;
     // diagnostics scratch
     long long *diag_out = nullptr;
     unsigned long long *diag_count = nullptr;
@@ -130,6 +135,8 @@ void release_device(bs_sim *s)
     s->diag_count = nullptr;
     s->diag_cap = 0;
     s->staging = nullptr;
+    s->cl_start_d = nullptr;
+    s->cl_sys_d = nullptr;
     if (s->ctl_host)
     {
         cudaFreeHost(s->ctl_host);
@@ -308,6 +315,132 @@ int capture_period_graph(bs_sim *s)
     if (e != cudaSuccess)
         return cuda_fail(s, e, "cudaGraphInstantiate");
     s->period_kernels = kernels;
+    return BS_OK;
+}
+
+// Assigns whole systems to the clusters of the persistent batched kernel: as many clusters as
+// can be resident at once for the current shape, systems in decreasing order of work each given
+// to the least-loaded cluster (longest-processing-time rule). Work of a system: its particles plus
+// its directed spring entries.
+int assign_clusters(bs_sim *s)
+{
+    Params &p = s->p;
+    int maxc = 0;
+    BS_CUDA(batch_max_clusters(p, s->shape, &maxc));
+    if (maxc < 1)
+        return fail(s, BS_E_ARG, "batch shape does not fit on the device (block " + std::to_string(s->shape.block) +
+                                     ", cluster " + std::to_string(s->shape.cluster) + ")");
+    const int nsys = p.nsys;
+    const int ncl = std::max(1, std::min(maxc, nsys));
+    std::vector<long long> cost(nsys, 0);
+    std::vector<int> deg(s->n, 0);
+    for (size_t t = 0; t < s->sp_i.size(); ++t)
+    {
+        deg[s->sp_i[t]]++;
+        deg[s->sp_j[t]]++;
+    }
+    for (int b = 0; b < nsys; ++b)
+        for (int64_t i = s->sys_off[b]; i < s->sys_off[b + 1]; ++i)
+            cost[b] += 1 + deg[i];
+    std::vector<int> order(nsys);
+    for (int b = 0; b < nsys; ++b)
+        order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::vector<long long> load(ncl, 0);
+    std::vector<std::vector<int>> lists(ncl);
+    for (int b : order)
+    {
+        int best = 0;
+        for (int c = 1; c < ncl; ++c)
+            if (load[c] < load[best])
+                best = c;
+        load[best] += cost[b];
+        lists[best].push_back(b);
+    }
+    std::vector<int> start(ncl + 1, 0), sys;
+    for (int c = 0; c < ncl; ++c)
+    {
+        start[c + 1] = start[c] + static_cast<int>(lists[c].size());
+        sys.insert(sys.end(), lists[c].begin(), lists[c].end());
+    }
+    BS_CUDA(cudaMemcpyAsync(s->cl_start_d, start.data(), sizeof(int) * (ncl + 1), cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(s->cl_sys_d, sys.data(), sizeof(int) * nsys, cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaStreamSynchronize(s->stream));
+    p.ncl = ncl;
+    destroy_graph(s);
+    return BS_OK;
+}
+
+// One period of a batched ensemble: rebuild, then the persistent kernel for K nominal steps.
+int capture_batch_graph(bs_sim *s)
+{
+    destroy_graph(s);
+    const int K = std::max(1, s->cfg.rebuild_every);
+    cudaGraph_t g = nullptr;
+    BS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int kernels = launch_rebuild(s->p, s->stream);
+    const cudaError_t le = launch_batch_run(s->p, s->shape, K, s->stream);
+    kernels += 1 + launch_batch_finish(s->p, K, s->stream);
+    const cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+    if (le != cudaSuccess)
+    {
+        if (g)
+            cudaGraphDestroy(g);
+        return cuda_fail(s, le, "batched step launch");
+    }
+    if (ce != cudaSuccess)
+        return cuda_fail(s, ce, "cudaStreamEndCapture");
+    const cudaError_t e = cudaGraphInstantiate(&s->period_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+        return cuda_fail(s, e, "cudaGraphInstantiate");
+    s->period_kernels = kernels;
+    return BS_OK;
+}
+
+// Enqueues `count` nominal steps of a batched ensemble on the rebuild schedule of the single-system
+// path; `catchup` first lets systems that stopped on a stale list reach the nominal count.
+int enqueue_batch(bs_sim *s, long long count, bool catchup)
+{
+    const int K = std::max(1, s->cfg.rebuild_every);
+    if (catchup)
+    {
+        s->launches += launch_rebuild(s->p, s->stream);
+        BS_CUDA(launch_batch_run(s->p, s->shape, 0, s->stream));
+        s->launches += 1 + launch_batch_finish(s->p, 0, s->stream);
+        s->list_valid = true;
+    }
+    long long remaining = count;
+    while (remaining > 0)
+    {
+        if (!s->list_valid || s->since_rebuild >= K)
+        {
+            if (remaining >= K)
+            {
+                if (!s->period_graph)
+                {
+                    const int rc = capture_batch_graph(s);
+                    if (rc)
+                        return rc;
+                }
+                BS_CUDA(cudaGraphLaunch(s->period_graph, s->stream));
+                s->launches += s->period_kernels;
+                s->list_valid = true;
+                s->since_rebuild = K;
+                remaining -= K;
+                continue;
+            }
+            s->launches += launch_rebuild(s->p, s->stream);
+            s->list_valid = true;
+            s->since_rebuild = 0;
+        }
+        const int chunk = static_cast<int>(std::min<long long>(remaining, K - s->since_rebuild));
+        BS_CUDA(launch_batch_run(s->p, s->shape, chunk, s->stream));
+        s->launches += 1 + launch_batch_finish(s->p, chunk, s->stream);
+        s->since_rebuild += chunk;
+        remaining -= chunk;
+    }
+    BS_CUDA(cudaGetLastError());
     return BS_OK;
 }
 
@@ -501,6 +634,26 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
         return fail(s, BS_E_STATE, "rigid-body dynamics are not available in this build");
     if (s->n == 0)
         return fail(s, BS_E_ARG, "bs_setup: no particles");
+    const bool batch = !s->sys_off.empty();
+    int max_sys = static_cast<int>(s->n);
+    if (batch)
+    {
+        if (s->sys_off.back() != s->n)
+            return fail(s, BS_E_ARG, "bs_set_systems: the offsets must end at the particle count");
+        if (!s->bodies.empty())
+            return fail(s, BS_E_ARG, "rigid bodies are not available for batched ensembles");
+        std::vector<int> sys_of_id(s->n);
+        max_sys = 0;
+        for (size_t b = 0; b + 1 < s->sys_off.size(); ++b)
+        {
+            max_sys = std::max(max_sys, static_cast<int>(s->sys_off[b + 1] - s->sys_off[b]));
+            for (int64_t i = s->sys_off[b]; i < s->sys_off[b + 1]; ++i)
+                sys_of_id[i] = static_cast<int>(b);
+        }
+        for (size_t t = 0; t < s->sp_i.size(); ++t)
+            if (sys_of_id[s->sp_i[t]] != sys_of_id[s->sp_j[t]])
+                return fail(s, BS_E_ARG, "a spring joins particles of two systems of the batch");
+    }
 
     release_device(s);
     s->cfg = c;
@@ -658,32 +811,74 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
             list_radius = std::max(list_radius, R);
     }
     p.list_radius = static_cast<float>(list_radius);
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int64_t i = 0; i < n; ++i)
+    // grid cells and density from the bounding box of each system (one system unless batched)
+    const int nsys = batch ? static_cast<int>(s->sys_off.size() - 1) : 1;
+    double cells = 0.0, density = 0.0;
+    for (int b = 0; b < nsys; ++b)
+    {
+        const int64_t i0 = batch ? s->sys_off[b] : 0, i1 = batch ? s->sys_off[b + 1] : n;
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int64_t i = i0; i < i1; ++i)
+            for (int k = 0; k < 3; ++k)
+            {
+                lo[k] = std::min(lo[k], static_cast<double>(s->xyz[3 * i + k]));
+                hi[k] = std::max(hi[k], static_cast<double>(s->xyz[3 * i + k]));
+            }
+        double c3 = 1.0, volume = 1.0;
         for (int k = 0; k < 3; ++k)
         {
-            lo[k] = std::min(lo[k], static_cast<double>(s->xyz[3 * i + k]));
-            hi[k] = std::max(hi[k], static_cast<double>(s->xyz[3 * i + k]));
+            c3 *= std::ceil((hi[k] - lo[k]) / (list_radius / kGridDiv)) + 3.0;
+            volume *= std::max(hi[k] - lo[k], 1.0);
         }
-    double cells = 1.0, volume = 1.0;
-    for (int k = 0; k < 3; ++k)
-    {
-        cells *= std::ceil((hi[k] - lo[k]) / (list_radius / kGridDiv)) + 3.0;
-        volume *= std::max(hi[k] - lo[k], 1.0);
+        cells += c3;
+        density = std::max(density, static_cast<double>(i1 - i0) / volume);
     }
     const int cell_cap = static_cast<int>(std::min(2.0 * cells + 1024.0, 2.0e8));
     // first capacity: 1.5x the mean count expected in the list sphere, at least 32
     int caps[kLists];
-    const double density = static_cast<double>(n) / volume;
     for (int t = 0; t < kLists; ++t)
     {
         const double R = static_cast<float>(cut[t]) + skin;
         const double expect = density * 4.18879 * R * R * R;
         caps[t] = static_cast<int>(std::min(std::max(1.5 * expect + 16.0, 32.0), 4096.0));
     }
+    if (batch && max_sys > 32768)
+        p.pl16 = 0; // offsets inside a system would not fit 16 bits
     int rc = alloc_lists(s, caps, cell_cap);
     if (rc)
         return rc;
+    if (batch)
+    {
+        p.nsys = nsys;
+        std::vector<int> start(nsys + 1), of(npad, 0);
+        for (int b = 0; b <= nsys; ++b)
+            start[b] = static_cast<int>(s->sys_off[b]);
+        for (int b = 0; b < nsys; ++b)
+            for (int i = start[b]; i < start[b + 1]; ++i)
+                of[i] = b;
+        int *d_start, *d_of;
+        BS_CUDA(s->dev.alloc(&d_start, nsys + 1));
+        BS_CUDA(s->dev.alloc(&d_of, npad));
+        p.sys_start = d_start;
+        p.sys_of = d_of;
+        BS_CUDA(s->dev.alloc(&p.sys_grid, nsys));
+        BS_CUDA(s->dev.alloc(&p.sys_cells, nsys + 1));
+        BS_CUDA(s->dev.alloc(&p.sys_status, nsys));
+        BS_CUDA(s->dev.alloc(&p.sys_steps, nsys));
+        BS_CUDA(s->dev.alloc(&p.stale_at, nsys));
+        BS_CUDA(s->dev.alloc(&p.sys_energy, static_cast<size_t>(nsys) * 8));
+        BS_CUDA(s->dev.alloc(&p.sys_part, static_cast<size_t>(nsys) * kMaxCluster * 16));
+        BS_CUDA(s->dev.alloc(&s->cl_start_d, nsys + 1));
+        BS_CUDA(s->dev.alloc(&s->cl_sys_d, nsys));
+        p.cl_start = s->cl_start_d;
+        p.cl_sys = s->cl_sys_d;
+        BS_CUDA(cudaMemcpyAsync(d_start, start.data(), sizeof(int) * (nsys + 1), cudaMemcpyHostToDevice, s->stream));
+        BS_CUDA(cudaMemcpyAsync(d_of, of.data(), sizeof(int) * npad, cudaMemcpyHostToDevice, s->stream));
+        BS_CUDA(cudaMemsetAsync(p.sys_status, 0, sizeof(int) * nsys, s->stream));
+        BS_CUDA(cudaMemsetAsync(p.sys_steps, 0, sizeof(long long) * nsys, s->stream));
+        BS_CUDA(cudaMemsetAsync(p.sys_energy, 0, sizeof(double) * nsys * 8, s->stream));
+        BS_CUDA(cudaMemsetAsync(p.stale_at, 0x7f, sizeof(long long) * nsys, s->stream));
+    }
 
     // ---- uploads ----
     BS_CUDA(cudaMemcpyAsync(p.pos[0], pos0.data(), sizeof(float4) * npad, cudaMemcpyHostToDevice, s->stream));
@@ -759,6 +954,15 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     s->steps_done = 0;
     s->target = 0;
     s->list_valid = false;
+    if (batch)
+    {
+        rc = assign_clusters(s);
+        if (rc)
+        {
+            s->ready = false;
+            return rc;
+        }
+    }
     rc = rebuild_now(s);
     if (rc)
     {
@@ -819,7 +1023,57 @@ int bs_step_async(bs_sim *s, int32_t nsteps)
     if (rc)
         return rc;
     s->target += nsteps;
+    if (s->p.nsys > 0)
+        return enqueue_batch(s, nsteps, false);
     return enqueue_steps(s, nsteps);
+}
+
+// Completes the queued work of a batched ensemble: repairs capacity overflows, lets systems
+// stopped by a stale list catch up, and reports the first system with a non-finite position.
+static int synchronize_batch(bs_sim *s)
+{
+    for (int round = 0; round < 64; ++round)
+    {
+        int rc = read_ctl(s);
+        if (rc)
+            return rc;
+        const Ctl &h = *s->ctl_host;
+        s->steps_done = h.nominal;
+        if (h.status & ST_NONFINITE)
+        {
+            std::vector<int> st(s->p.nsys);
+            BS_CUDA(cudaMemcpy(st.data(), s->p.sys_status, sizeof(int) * st.size(), cudaMemcpyDeviceToHost));
+            int first = -1;
+            for (size_t b = 0; b < st.size() && first < 0; ++b)
+                if (st[b] & ST_NONFINITE)
+                    first = static_cast<int>(b);
+            return fail(s, BS_E_NONFINITE,
+                        "Found non-finite position in system " + std::to_string(first) + " of the batch");
+        }
+        if (h.status & (ST_CELL_CAPACITY | ST_PAIR_CAPACITY | ST_WIDE))
+        {
+            rc = rebuild_now(s);
+            if (rc)
+                return rc;
+            continue;
+        }
+        if (h.nominal < s->target)
+        {
+            rc = enqueue_batch(s, s->target - h.nominal, false);
+            if (rc)
+                return rc;
+            continue;
+        }
+        if (h.lagging > 0)
+        {
+            rc = enqueue_batch(s, 0, true);
+            if (rc)
+                return rc;
+            continue;
+        }
+        return BS_OK;
+    }
+    return fail(s, BS_E_STATE, "bs_synchronize: the batch could not complete the requested steps");
 }
 
 int bs_synchronize(bs_sim *s)
@@ -828,6 +1082,8 @@ int bs_synchronize(bs_sim *s)
         return fail(nullptr, BS_E_ARG, "null handle");
     if (!s->ready)
         return fail(s, BS_E_STATE, "call bs_setup first");
+    if (s->p.nsys > 0)
+        return synchronize_batch(s);
     for (int round = 0; round < 64; ++round)
     {
         int rc = read_ctl(s);
@@ -911,6 +1167,8 @@ int bs_set_external_forces(bs_sim *s, const float *f)
         return fail(nullptr, BS_E_ARG, "null handle");
     if (!s->ready)
         return fail(s, BS_E_STATE, "call bs_setup first");
+    if (s->p.nsys > 0)
+        return fail(s, BS_E_STATE, "external forces are not available for batched ensembles");
     if (!f)
         return fail(s, BS_E_ARG, "bs_set_external_forces: null forces");
     for (int64_t i = 0; i < s->n; ++i)
@@ -1005,6 +1263,8 @@ int bs_set_force(bs_sim *s, int64_t i, const float f[3])
         return fail(nullptr, BS_E_ARG, "null handle");
     if (!s->ready)
         return fail(s, BS_E_STATE, "call bs_setup first");
+    if (s->p.nsys > 0)
+        return fail(s, BS_E_STATE, "external forces are not available for batched ensembles");
     if (i < 0 || i >= s->n || !f)
         return fail(s, BS_E_ARG, "bs_set_force: particle index out of range");
     s->ext_host[i].x += f[0];
@@ -1039,6 +1299,8 @@ int bs_get_pairs(bs_sim *s, int32_t term, int64_t *out, int64_t cap, int64_t *n_
         return fail(s, BS_E_STATE, "call bs_setup first");
     if (term < BS_TERM_STERIC || term > BS_TERM_HYDROPHOBIC || cap < 0 || !n_out || (cap > 0 && !out))
         return fail(s, BS_E_ARG, "bs_get_pairs: bad arguments");
+    if (s->p.nsys > 0)
+        return fail(s, BS_E_STATE, "pair and cell diagnostics are for single systems");
     {
         const int rc = settle(s);
         if (rc)
@@ -1093,6 +1355,8 @@ int bs_get_cells(bs_sim *s, int32_t term, int64_t *out)
         return fail(s, BS_E_STATE, "call bs_setup first");
     if (term < BS_TERM_STERIC || term > BS_TERM_HYDROPHOBIC || !out)
         return fail(s, BS_E_ARG, "bs_get_cells: bad arguments");
+    if (s->p.nsys > 0)
+        return fail(s, BS_E_STATE, "pair and cell diagnostics are for single systems");
     {
         const int rc = settle(s);
         if (rc)
@@ -1131,6 +1395,196 @@ int bs_get_cells(bs_sim *s, int32_t term, int64_t *out)
     BS_CUDA(cudaGetLastError());
     BS_CUDA(cudaMemcpyAsync(out, d_out, sizeof(int64_t) * s->n, cudaMemcpyDeviceToHost, s->stream));
     BS_CUDA(cudaStreamSynchronize(s->stream));
+    return BS_OK;
+}
+
+int bs_set_systems(bs_sim *s, int32_t nsys, const int64_t *offsets)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (nsys < 0 || (nsys > 0 && !offsets))
+        return fail(s, BS_E_ARG, "bs_set_systems: bad arguments");
+    if (nsys == 0)
+    {
+        s->sys_off.clear();
+        s->ready = false;
+        return BS_OK;
+    }
+    if (offsets[0] != 0)
+        return fail(s, BS_E_ARG, "bs_set_systems: the first offset must be 0");
+    for (int32_t b = 0; b < nsys; ++b)
+        if (offsets[b + 1] <= offsets[b])
+            return fail(s, BS_E_ARG, "bs_set_systems: every system needs at least one particle");
+    s->sys_off.assign(offsets, offsets + nsys + 1);
+    s->ready = false;
+    return BS_OK;
+}
+
+int bs_set_batch_shape(bs_sim *s, int32_t block, int32_t lanes, int32_t cluster)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!(block == 128 || block == 256 || block == 512) || !(lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8) ||
+        !(cluster == 1 || cluster == 2 || cluster == 4 || cluster == 8))
+        return fail(s, BS_E_ARG, "bs_set_batch_shape: block in {128, 256, 512}, lanes in {1, 2, 4, 8}, cluster in {1, 2, 4, 8}");
+    const BatchShape old = s->shape;
+    s->shape = BatchShape{block, lanes, cluster};
+    if (s->ready && s->p.nsys > 0)
+    {
+        int rc = bs_synchronize(s);
+        if (rc == BS_OK)
+            rc = assign_clusters(s);
+        if (rc)
+        {
+            s->shape = old;
+            return rc;
+        }
+    }
+    return BS_OK;
+}
+
+int bs_get_batch_shape(bs_sim *s, int32_t shape[3])
+{
+    if (!s || !shape)
+        return fail(s, BS_E_ARG, "bs_get_batch_shape: null argument");
+    shape[0] = s->shape.block;
+    shape[1] = s->shape.lanes;
+    shape[2] = s->shape.cluster;
+    return BS_OK;
+}
+
+int bs_batch_autotune(bs_sim *s, int32_t shape[3])
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready || s->p.nsys == 0)
+        return fail(s, BS_E_STATE, "bs_batch_autotune: set up a batched ensemble first");
+    int rc = bs_synchronize(s);
+    if (rc)
+        return rc;
+    if (!s->list_valid)
+    {
+        rc = rebuild_now(s);
+        if (rc)
+            return rc;
+    }
+    Params &p = s->p;
+    const size_t np = static_cast<size_t>(p.npad), ns = static_cast<size_t>(p.nsys);
+    // Trials step the real state; it is saved here and put back after every trial.
+    DeviceBuffers save;
+    float4 *sv[4];
+    long long *s_steps, *s_stale;
+    int *s_status;
+    double *s_energy;
+    for (int k = 0; k < 4; ++k)
+        BS_CUDA(save.alloc(&sv[k], np));
+    BS_CUDA(save.alloc(&s_steps, ns));
+    BS_CUDA(save.alloc(&s_stale, ns));
+    BS_CUDA(save.alloc(&s_status, ns));
+    BS_CUDA(save.alloc(&s_energy, ns * 8));
+    float4 *live[4] = {p.pos[0], p.pos[1], p.vel[0], p.vel[1]};
+    auto copy_all = [&](bool to_save) -> cudaError_t {
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+            e = cudaMemcpyAsync(to_save ? sv[k] : live[k], to_save ? live[k] : sv[k], sizeof(float4) * np,
+                                cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(to_save ? s_steps : p.sys_steps, to_save ? p.sys_steps : s_steps, sizeof(long long) * ns,
+                                cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(to_save ? s_stale : p.stale_at, to_save ? p.stale_at : s_stale, sizeof(long long) * ns,
+                                cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(to_save ? s_status : p.sys_status, to_save ? p.sys_status : s_status, sizeof(int) * ns,
+                                cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(to_save ? s_energy : p.sys_energy, to_save ? p.sys_energy : s_energy,
+                                sizeof(double) * ns * 8, cudaMemcpyDeviceToDevice, s->stream);
+        return e;
+    };
+    cudaError_t e = copy_all(true);
+    if (e != cudaSuccess)
+    {
+        save.free_all();
+        return cuda_fail(s, e, "bs_batch_autotune: saving the state");
+    }
+    cudaEvent_t ev[2];
+    cudaEventCreate(&ev[0]);
+    cudaEventCreate(&ev[1]);
+    const int K = std::max(1, s->cfg.rebuild_every);
+    const BatchShape old = s->shape;
+    BatchShape best = old;
+    float best_ms = 1e30f;
+    const int blocks[3] = {128, 256, 512}, lanes[3] = {2, 4, 8}, clusters[4] = {1, 2, 4, 8};
+    for (int cb : clusters)
+        for (int bb : blocks)
+            for (int lb : lanes)
+            {
+                s->shape = BatchShape{bb, lb, cb};
+                if (assign_clusters(s) != BS_OK)
+                    continue;
+                float ms = 1e30f;
+                for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep)
+                {
+                    e = cudaEventRecord(ev[0], s->stream);
+                    if (e == cudaSuccess)
+                        e = launch_batch_run(p, s->shape, K, s->stream);
+                    if (e == cudaSuccess)
+                        e = cudaEventRecord(ev[1], s->stream);
+                    if (e == cudaSuccess)
+                        e = cudaEventSynchronize(ev[1]);
+                    float t = 0.f;
+                    if (e == cudaSuccess)
+                        e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+                    if (e == cudaSuccess)
+                        e = copy_all(false);
+                    ms = std::min(ms, t);
+                }
+                if (e != cudaSuccess)
+                    break;
+                if (ms < best_ms)
+                {
+                    best_ms = ms;
+                    best = s->shape;
+                }
+            }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    if (e == cudaSuccess)
+        e = copy_all(false);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s->stream);
+    save.free_all();
+    if (e != cudaSuccess)
+        return cuda_fail(s, e, "bs_batch_autotune: trial run");
+    s->shape = best;
+    rc = assign_clusters(s);
+    if (rc)
+        return rc;
+    if (shape)
+    {
+        shape[0] = best.block;
+        shape[1] = best.lanes;
+        shape[2] = best.cluster;
+    }
+    return BS_OK;
+}
+
+int bs_get_system_energies(bs_sim *s, double *out)
+{
+    if (!s || !out)
+        return fail(s, BS_E_ARG, "bs_get_system_energies: null argument");
+    if (!s->ready || s->p.nsys == 0)
+        return fail(s, BS_E_STATE, "bs_get_system_energies: set up a batched ensemble first");
+    int rc = bs_synchronize(s);
+    if (rc)
+        return rc;
+    const int nsys = s->p.nsys;
+    std::vector<double> e(static_cast<size_t>(nsys) * 8);
+    BS_CUDA(cudaMemcpy(e.data(), s->p.sys_energy, sizeof(double) * e.size(), cudaMemcpyDeviceToHost));
+    for (int b = 0; b < nsys; ++b)
+        for (int k = 0; k < BS_NUM_ENERGIES; ++k)
+            out[static_cast<size_t>(b) * BS_NUM_ENERGIES + k] = e[static_cast<size_t>(b) * 8 + k];
     return BS_OK;
 }
 

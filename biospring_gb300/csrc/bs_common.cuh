@@ -82,6 +82,19 @@ struct Ctl
     int status_pending;        // bits raised during a step, merged into status by its last block
     int ext_pending;           // an external force waits in Params::ext
     double energies[8];        // BS_ENERGY_* of the last evaluation
+    // batched ensembles
+    long long nominal;         // steps every system should have completed after the queued work
+    int lagging;               // live systems behind `nominal` (stopped early by a stale list)
+    int dead;                  // systems with a non-finite position
+};
+
+// Search grid of one system of a batched ensemble (same formula as the single-system grid).
+struct SysGrid
+{
+    double gmin[3];
+    float radius;
+    int nx, ny, nz;
+    int cells;
 };
 
 // One typed pair list, row-major [slot * cap + k]: entries = slot | kEntryStatic, or for
@@ -157,6 +170,24 @@ struct Params
     float k_kin;              // kKineticConvert
     float k_imp_f;            // kImpForceConvert
     float k_hydro_e;          // N_A * 1e-3
+    // batched ensembles (nsys = 0: one system). Every system keeps a fixed, contiguous range of
+    // slots in every layout: its cells are numbered after the previous system's, so the sort by
+    // cell never mixes systems, and its pair lists and springs stay inside the range.
+    int nsys;
+    const int *sys_start;     // [nsys + 1] slot ranges
+    const int *sys_of;        // [npad] system of each slot (0 for padding)
+    SysGrid *sys_grid;        // [nsys]
+    int *sys_cells;           // [nsys + 1] first global cell of each system
+    int *sys_status;          // [nsys] ST_NONFINITE / ST_STALE raised by the system
+    long long *sys_steps;     // [nsys] steps completed by each system
+    long long *stale_at;      // [nsys] first step whose end positions left the list skin
+    double *sys_energy;       // [nsys * 8] BS_ENERGY_* of each system's last step
+    float *sys_part;          // [nsys * kMaxCluster * 16] per-block energy partials (hi, lo)
+    const int *cl_start;      // [ncl + 1] systems of each cluster of the persistent kernel
+    const int *cl_sys;        // [nsys]
+    int ncl;
 };
+
+constexpr int kMaxCluster = 16;
 
 } // namespace bsg

@@ -1,0 +1,586 @@
+// bs_device.cuh -- device functions shared by the single-system and the batched kernels:
+// order-preserving float codes, own reciprocal and square-root refinements, the reference's
+// cell coordinate and exact pair test, compensated energy sums, and the per-particle force and
+// integration routine of one step.
+#pragma once
+
+#include <cfloat>
+#include <climits>
+
+#include "bs_kernels.cuh"
+
+namespace bsg
+{
+namespace
+{
+
+
+__device__ __forceinline__ int status_of(const Ctl *c) { return *(volatile const int *)&c->status; }
+
+__device__ __forceinline__ unsigned int f2ord(float f)
+{
+    const unsigned int b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned int u)
+{
+    const unsigned int b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    return __uint_as_float(b);
+}
+
+// 1/x: hardware approximation refined by one Newton-Raphson step for f(r) = 1/r - x,
+// r1 = r0 + r0 (1 - x r0); about one unit in the last place for normal x.
+__device__ __forceinline__ float recip_nr(float x)
+{
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return fmaf(r, fmaf(-x, r, 1.0f), r);
+}
+
+// 1/sqrt(x): hardware approximation refined by one Newton-Raphson step for
+// f(r) = 1/r^2 - x, r1 = r0 (3 - x r0^2) / 2.
+__device__ __forceinline__ float rsqrt_nr(float x)
+{
+    float r;
+    asm("rsqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r * fmaf(-0.5f * x, r * r, 1.5f);
+}
+
+// Reference cell coordinate along one axis: (size_t)((x - min) / radius), clamped (nsearch.hpp:282-289).
+__device__ __forceinline__ int ref_cell_coord(float x, double mn, float radius, int ncell)
+{
+    const double t = __ddiv_rn(__dsub_rn(static_cast<double>(x), mn), static_cast<double>(radius));
+    unsigned long long c = static_cast<unsigned long long>(t);
+    const unsigned long long lim = static_cast<unsigned long long>(ncell - 1);
+    return static_cast<int>(c < lim ? c : lim);
+}
+
+// Search grid over the box [mn, mx] with cell edge `edge`: ncells = ceil(len / edge) + 1 per
+// axis in FP64 (nsearch.hpp:351-354), minimum corner as double. Returns the total cell count as a
+// double (it can exceed the int range; the per-axis counts saturate at 1e9).
+__device__ __forceinline__ double grid_dims(const float (&mn)[3], const float (&mx)[3], float edge, double (&gmin)[3],
+                                            int (&nc)[3])
+{
+    const double r = static_cast<double>(edge);
+    double cells = 1.0;
+    for (int k = 0; k < 3; ++k)
+    {
+        const double len = __dsub_rn(static_cast<double>(mx[k]), static_cast<double>(mn[k]));
+        const double c = ceil(__ddiv_rn(len, r)) + 1.0;
+        cells *= c;
+        nc[k] = c < 1.0e9 ? static_cast<int>(c) : 1000000000;
+        gmin[k] = static_cast<double>(mn[k]);
+    }
+    return cells;
+}
+
+// Exact reference test of one candidate pair for one cutoff: the grid filter compares the FP64
+// distance of the float coordinates (nsearch.hpp:230, measure.hpp:163-169); the force routine
+// then compares the float-rounded FP64 norm of the float difference vector (Particle.cpp:222-224,
+// Vector3f.cpp:9-12, measure.hpp:188-196). Only pairs inside the guard band come here.
+__device__ __noinline__ bool exact_pair_test(float4 pi, float4 pj, float cutoff, bool nonzero)
+{
+    const double ax = __dsub_rn(static_cast<double>(pi.x), static_cast<double>(pj.x));
+    const double ay = __dsub_rn(static_cast<double>(pi.y), static_cast<double>(pj.y));
+    const double az = __dsub_rn(static_cast<double>(pi.z), static_cast<double>(pj.z));
+    const double s = __dadd_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)), __dmul_rn(az, az));
+    if (!(__dsqrt_rn(s) < static_cast<double>(cutoff)))
+        return false;
+    const double fx = static_cast<double>(__fsub_rn(pj.x, pi.x));
+    const double fy = static_cast<double>(__fsub_rn(pj.y, pi.y));
+    const double fz = static_cast<double>(__fsub_rn(pj.z, pi.z));
+    double nrm = 0.0;
+    if (!(fabs(fx) < 1e-40 && fabs(fy) < 1e-40 && fabs(fz) < 1e-40))
+        nrm = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fy, fy)), __dmul_rn(fz, fz)));
+    const float d = __double2float_rn(nrm);
+    if (!(d < cutoff))
+        return false;
+    if (nonzero && !(d != 0.0f))
+        return false;
+    return true;
+}
+
+// Classifies a pair for one term. Outside the band [lo2, hi2) the FP32 squared distance decides
+// (its error is far below the band); inside it, and for (near-)coincident particles, the exact
+// reference test decides.
+__device__ __forceinline__ bool pair_in(float r2, float lo2, float hi2, float4 pi, float4 pj, float cutoff,
+                                        bool nonzero)
+{
+    if (r2 >= hi2)
+        return false;
+    if (r2 < lo2 && r2 > 1e-20f)
+        return true;
+    return exact_pair_test(pi, pj, cutoff, nonzero);
+}
+
+// Knuth's TwoSum: s = fl(a + b) and s + err == a + b exactly (round-to-nearest, no contraction).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &err)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (hi, lo) += (h2, l2) in float-float (double-single) arithmetic: about 44 significant bits.
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float h2, float l2)
+{
+    float s, e;
+    two_sum(hi, h2, s, e);
+    e = __fadd_rn(e, __fadd_rn(lo, l2));
+    two_sum(s, e, hi, lo);
+}
+
+// Deterministic reduction of NE per-thread float partials over the grid. Warp sums are FP32
+// trees, block sums float-float (compensated), the block partials are stored as (hi, lo) pairs, and the
+// last block to finish sums them in block order, also float-float, and writes the totals as
+// double. The result carries the accuracy of an FP64 reduction without using the FP64 pipe,
+// which runs at a small fraction of the FP32 rate on this part.
+template <int NE, int BLOCK>
+__device__ __forceinline__ bool reduce_energies(const float (&e)[NE], double *blk_d, unsigned int *done, double *dst)
+{
+    float *blk = reinterpret_cast<float *>(blk_d); // [block][16]: (hi, lo) per energy
+    __shared__ float shh[NE][BLOCK / 32], shl[NE][BLOCK / 32];
+    __shared__ bool am_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NE; ++k)
+    {
+        // 32 terms: a plain FP32 tree keeps ~1e-7 relative; compensation starts above the warp
+        float v = e[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0)
+        {
+            shh[k][warp] = v;
+            shl[k][warp] = 0.0f;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < NE)
+    {
+        float hi = 0.0f, lo = 0.0f;
+        for (int w = 0; w < BLOCK / 32; ++w)
+            ff_add(hi, lo, shh[threadIdx.x][w], shl[threadIdx.x][w]);
+        blk[static_cast<size_t>(blockIdx.x) * 16 + 2 * threadIdx.x] = hi;
+        blk[static_cast<size_t>(blockIdx.x) * 16 + 2 * threadIdx.x + 1] = lo;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0)
+        am_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!am_last)
+        return false;
+    __threadfence();
+    for (int k = 0; k < NE; ++k)
+    {
+        float hi = 0.0f, lo = 0.0f;
+        for (unsigned int b = threadIdx.x; b < gridDim.x; b += BLOCK)
+            ff_add(hi, lo, __ldcg(&blk[static_cast<size_t>(b) * 16 + 2 * k]),
+                   __ldcg(&blk[static_cast<size_t>(b) * 16 + 2 * k + 1]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
+            const float l2 = __shfl_down_sync(0xffffffffu, lo, o);
+            ff_add(hi, lo, h2, l2);
+        }
+        __syncthreads();
+        if (lane == 0)
+        {
+            shh[0][warp] = hi;
+            shl[0][warp] = lo;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            float th = 0.0f, tl = 0.0f;
+            for (int w = 0; w < BLOCK / 32; ++w)
+                ff_add(th, tl, shh[0][w], shl[0][w]);
+            dst[k] = static_cast<double>(th) + static_cast<double>(tl);
+        }
+    }
+    if (threadIdx.x == 0)
+        *done = 0u;
+    return true;
+}
+
+// Springs of slot s handled by lane t of T (Spring.cpp:20-34, spring.hpp:17-29). Returns the
+// force before the unit conversion and scale, and the weighted energy before the scale.
+template <int T>
+__device__ __forceinline__ void spring_forces(const Params &p, int s, int t, float4 pi,
+                                              const float4 *__restrict__ pos, float &fx, float &fy, float &fz,
+                                              float &e)
+{
+    const int deg = p.se_deg[s];
+    const size_t stride = static_cast<size_t>(p.npad);
+    for (int k = t; k < deg; k += T)
+    {
+        const size_t at = static_cast<size_t>(k) * stride + s;
+        const unsigned int c = __ldg(&p.se_col[at]);
+        if (c & kEntryInactive)
+            continue;
+        const float4 pj = __ldg(&pos[c & kSlotMask]);
+        const float kk = __ldg(&p.se_k[at]), r0 = __ldg(&p.se_r0[at]);
+        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float inv = r2 > 0.0f ? rsqrt_nr(r2) : 0.0f;
+        const float len = r2 * inv;
+        const float dv = len - r0;
+        const float w = (c & kEntryStatic) ? 1.0f : 0.5f;
+        e = fmaf(w * 0.5f * kk, dv * dv, e);
+        const float fod = kk * dv * inv;
+        fx = fmaf(dx, fod, fx);
+        fy = fmaf(dy, fod, fy);
+        fz = fmaf(dz, fod, fz);
+    }
+}
+
+// Steric pairs of slot s handled by lane t of T (Particle.cpp:368-429, steric.hpp:27-156).
+// KIND 0: list 0 in 16-bit mode (partner = slot + offset, dynamic partners, half the pair
+// energy); KIND 1: list 0 in 32-bit mode; KIND 2: list 3 (static partners, full energy).
+// The loop is software-pipelined: entries are loaded two iterations ahead of use and
+// positions one iteration ahead.
+template <int SM, int T, int KIND>
+__device__ __forceinline__ void steric_forces(const Params &p, int s, int t, float4 pi, float fhi_i,
+                                              const float4 *__restrict__ pos, const float *__restrict__ fhi,
+                                              float &fx, float &fy, float &fz, float &e)
+{
+    const PairList &L = p.pl[KIND == 2 ? kListStericStatic : 0];
+    const int cnt = L.cnt[s];
+    if (t >= cnt)
+        return;
+    const size_t row = static_cast<size_t>(s) * L.cap;
+    const short *__restrict__ idx16 = reinterpret_cast<const short *>(L.idx) + row;
+    const unsigned int *__restrict__ idx32 = L.idx + row;
+    auto entry = [&](int k) -> int {
+        if (KIND == 0)
+            return s + static_cast<int>(__ldg(idx16 + k));
+        return static_cast<int>(__ldg(idx32 + k) & kSlotMask);
+    };
+    const float lo2 = p.lo2_s, hi2 = p.hi2_s;
+    const float w = KIND == 2 ? 1.0f : 0.5f;
+    int jn = entry(t);
+    int jn2 = t + T < cnt ? entry(t + T) : 0;
+    float4 pn = __ldg(&pos[jn]);
+    for (int k = t; k < cnt; k += T)
+    {
+        const int j = jn;
+        const float4 pj = pn;
+        jn = jn2;
+        if (k + 2 * T < cnt)
+            jn2 = entry(k + 2 * T);
+        if (k + T < cnt)
+            pn = __ldg(&pos[jn]);
+        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 >= hi2)
+            continue;
+        if (!(r2 < lo2 && r2 > 1e-20f) && !exact_pair_test(pi, pj, p.c_steric, false))
+            continue;
+        if (SM == BS_STERIC_LINEAR)
+        {
+            // steric.hpp:37-59: E = (d - (ri + rj))^2 / 2 when overlapping, |F| = |d - (ri + rj)|.
+            // d - (ri + rj) cancels near contact, so d is the correctly rounded square root here.
+            const float d = sqrtf(r2);
+            const float inv = d > 0.0f ? 1.0f / d : 0.0f;
+            const float dv = d - (pi.w + pj.w);
+            if (dv > 0.0f)
+                continue;
+            e = fmaf(w * 0.5f, dv * dv, e);
+            const float fod = dv * inv; // -|dv| / d
+            fx = fmaf(dx, fod, fx);
+            fy = fmaf(dy, fod, fy);
+            fz = fmaf(dz, fod, fz);
+        }
+        else
+        {
+            if (r2 < 0.01f) // d < 0.1 A: the LJ forms give zero (steric.hpp:71-72)
+                continue;
+            const float inv2 = recip_nr(r2);
+            const float i6 = inv2 * inv2 * inv2;
+            const float t6 = pi.w * pj.w * i6;
+            const float hj = __ldg(&fhi[j]);
+            float fod;
+            if (SM == BS_STERIC_LJ_12_6_AMBER)
+            {
+                const float t12 = fhi_i * hj * i6 * i6;
+                e = fmaf(w, t12 - 2.0f * t6, e);
+                fod = 12.0f * (t6 - t12) * inv2;
+            }
+            else if (SM == BS_STERIC_LJ_8_6_LEWITT)
+            {
+                const float t8 = fhi_i * hj * i6 * inv2;
+                e = fmaf(w, 3.0f * t8 - 4.0f * t6, e);
+                fod = 24.0f * (t6 - t8) * inv2;
+            }
+            else
+            {
+                const float t8 = fhi_i * hj * i6 * inv2;
+                e = fmaf(w, t8 - t6, e);
+                fod = (6.0f * t6 - 8.0f * t8) * inv2;
+            }
+            fx = fmaf(dx, fod, fx);
+            fy = fmaf(dy, fod, fy);
+            fz = fmaf(dz, fod, fz);
+        }
+    }
+}
+
+// Coulomb pairs of a charged slot, lane t of T (Particle.cpp:191-253, electrostatic.hpp:16-49).
+// With the distance-dependent dielectric eps = D r, E = K q q / (D r^2) and F = -dE/dr.
+template <int T>
+__device__ __forceinline__ void coulomb_forces(const Params &p, int s, int t, float4 pi, float qi,
+                                               const float4 *__restrict__ pos, const float *__restrict__ chg,
+                                               float &fx, float &fy, float &fz, float &e)
+{
+    const PairList &L = p.pl[1];
+    const int cnt = L.cnt[s];
+    const unsigned int *__restrict__ row = L.idx + static_cast<size_t>(s) * L.cap;
+    const bool dist = p.dielectric_mode == BS_DIELECTRIC_DISTANCE;
+    for (int k = t; k < cnt; k += T)
+    {
+        const unsigned int j = __ldg(row + k);
+        const float4 pj = __ldg(&pos[j & kSlotMask]);
+        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (!pair_in(r2, p.lo2_c, p.hi2_c, pi, pj, p.c_coulomb, true))
+            continue;
+        if (r2 < 1e-6f) // d < 0.001 A gives zero (electrostatic.hpp:18-19)
+            continue;
+        const float inv = rsqrt_nr(r2);
+        const float qq = qi * __ldg(&chg[j & kSlotMask]);
+        const float w = (j & kEntryStatic) ? 1.0f : 0.5f;
+        float tq = qq * inv;
+        float fod;
+        if (dist)
+        {
+            tq *= inv;
+            fod = -2.0f * tq * inv * inv;
+        }
+        else
+            fod = -tq * inv * inv;
+        e = fmaf(w, tq, e);
+        fx = fmaf(dx, fod, fx);
+        fy = fmaf(dy, fod, fy);
+        fz = fmaf(dz, fod, fz);
+    }
+}
+
+// Hydrophobic pairs, lane t of T (Particle.cpp:269-330, hydrophobic.hpp:20-39).
+template <int T>
+__device__ __forceinline__ void hydro_forces(const Params &p, int s, int t, float4 pi, float hi,
+                                             const float4 *__restrict__ pos, const float *__restrict__ hyd,
+                                             float &fx, float &fy, float &fz, float &e)
+{
+    const PairList &L = p.pl[2];
+    const int cnt = L.cnt[s];
+    const unsigned int *__restrict__ row = L.idx + static_cast<size_t>(s) * L.cap;
+    for (int k = t; k < cnt; k += T)
+    {
+        const unsigned int j = __ldg(row + k);
+        const float4 pj = __ldg(&pos[j & kSlotMask]);
+        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (!pair_in(r2, p.lo2_h, p.hi2_h, pi, pj, p.c_hydro, true))
+            continue;
+        const float inv = rsqrt_nr(r2);
+        const float d = r2 * inv;
+        const float x = hi * __ldg(&hyd[j & kSlotMask]) * expf(-d);
+        const float w = (j & kEntryStatic) ? 1.0f : 0.5f;
+        e = fmaf(-w, x, e);
+        const float fod = x * inv;
+        fx = fmaf(dx, fod, fx);
+        fy = fmaf(dy, fod, fy);
+        fz = fmaf(dz, fod, fz);
+    }
+}
+
+// Sum over the T consecutive lanes of a particle group (result in every lane of the group).
+template <int T> __device__ __forceinline__ float group_sum(float v)
+{
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// One particle of one step (or of one force evaluation), lane t of the T consecutive lanes that
+// share slot s: each lane takes every T-th entry of the particle's spring row and pair lists, the
+// group sums its partial forces with shuffles, and the group's first lane adds the per-particle
+// terms and integrates (reading buffer sb, writing sb ^ 1). Slots at or beyond `send` are
+// inactive. Every lane of the warp must call it (shuffles). Adds the particle's energies to
+// eacc (spring, steric, Coulomb, hydrophobic, IMPALA, kinetic) and returns the status bits it
+// raised (ST_NONFINITE, ST_STALE).
+template <int MODE, int SM, int T>
+__device__ __forceinline__ int particle_step(const Params &p, const int s, const int t, const int send,
+                                             const int sb, const int lb, const bool ext_on, float (&eacc)[6])
+{
+    const float4 *__restrict__ pos = p.pos[sb];
+    const bool lead = t == 0;
+    int pend = 0;
+
+    // energies: spring, steric, coulomb, hydrophobic, imp, kinetic
+    float e[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    unsigned int fi = PF_STATIC;
+    float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (s < send)
+    {
+        pi = pos[s];
+        fi = p.flags[lb][s];
+    }
+    const bool active = s < send && !(fi & PF_STATIC);
+    if (active)
+    {
+        if (p.spring_on)
+        {
+            float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+            spring_forces<T>(p, s, t, pi, pos, sx, sy, sz, es);
+            const float kf = p.k_spring_f * p.spring_scale;
+            fx = sx * kf;
+            fy = sy * kf;
+            fz = sz * kf;
+            e[0] = es * p.spring_scale;
+        }
+        if (p.steric_on)
+        {
+            float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+            const float fhi_i = p.fhi[lb][s];
+            if (p.pl16)
+                steric_forces<SM, T, 0>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
+            else
+                steric_forces<SM, T, 1>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
+            if (p.pl[kListStericStatic].cnt[s] > 0)
+                steric_forces<SM, T, 2>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
+            const float kf = p.k_spring_f * p.steric_scale;
+            fx = fmaf(sx, kf, fx);
+            fy = fmaf(sy, kf, fy);
+            fz = fmaf(sz, kf, fz);
+            e[1] = es * p.steric_scale;
+        }
+        if (p.coulomb_on && (fi & PF_CHARGED))
+        {
+            float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+            coulomb_forces<T>(p, s, t, pi, p.chg[lb][s], pos, p.chg[lb], sx, sy, sz, es);
+            fx = fmaf(sx, p.k_elec_f, fx);
+            fy = fmaf(sy, p.k_elec_f, fy);
+            fz = fmaf(sz, p.k_elec_f, fz);
+            e[2] = es * p.k_elec_e;
+        }
+        if (p.hydro_on && (fi & PF_HYDROPHOBIC))
+        {
+            float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+            hydro_forces<T>(p, s, t, pi, p.hyd[lb][s], pos, p.hyd[lb], sx, sy, sz, es);
+            const float kf = p.k_spring_f * p.hydro_scale;
+            fx = fmaf(sx, kf, fx);
+            fy = fmaf(sy, kf, fy);
+            fz = fmaf(sz, kf, fz);
+            e[3] = es * p.k_hydro_e * p.hydro_scale;
+        }
+    }
+    if (T > 1)
+    {
+        // every lane of the warp takes part in the group reductions
+        fx = group_sum<T>(fx);
+        fy = group_sum<T>(fy);
+        fz = group_sum<T>(fz);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            e[k] = group_sum<T>(e[k]);
+        if (!lead)
+        {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                e[k] = 0.f;
+        }
+    }
+    if (lead && s < send)
+    {
+        if (!active)
+        {
+            if (MODE == MODE_STEP)
+            {
+                p.pos[sb ^ 1][s] = pi;
+                p.vel[sb ^ 1][s] = p.vel[sb][s];
+            }
+            else
+                p.force_out[p.perm[lb][s]] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        else
+        {
+            const float4 v = p.vel[sb][s];
+            // ---- viscosity (Particle.cpp:80-84) ----
+            if (p.visc_on)
+            {
+                fx -= v.x * p.visc;
+                fy -= v.y * p.visc;
+                fz -= v.z * p.visc;
+            }
+            const float4 ip = p.iprm[lb][s];
+            // ---- IMPALA, flat membrane (imp.hpp:29-159, ForceField.cpp:62-88) ----
+            if (p.imp_on)
+            {
+                const float ex = expf(p.imp_alpha * (fabsf(pi.z) - p.imp_z0));
+                const float cz = 0.5f - 1.0f / (1.0f + ex);
+                const float gg = -ip.y * ip.z + kAlip * ip.y;
+                e[4] = p.imp_scale * gg * cz;
+                // dC/dz = alpha sign(z) e / (1 + e)^2, written without overflow
+                float dcz = pi.z != 0.0f ? p.imp_alpha / (ex + 2.0f + 1.0f / ex) : 0.0f;
+                if (pi.z < 0.0f)
+                    dcz = -dcz;
+                if (!isfinite(dcz))
+                    dcz = 0.0f;
+                fz -= p.imp_scale * (gg * dcz * p.k_imp_f);
+            }
+            // ---- external force (SpringNetwork::setForce, SpringNetwork.cpp:438-442) ----
+            if (ext_on)
+            {
+                const int id = p.perm[lb][s];
+                const float4 xf = p.ext[id];
+                fx += xf.x;
+                fy += xf.y;
+                fz += xf.z;
+                if (MODE == MODE_STEP && (xf.x != 0.f || xf.y != 0.f || xf.z != 0.f))
+                    p.ext[id] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            if (MODE == MODE_FORCES)
+            {
+                p.force_out[p.perm[lb][s]] = make_float4(fx, fy, fz, 0.f);
+            }
+            else
+            {
+                // ---- semi-implicit Euler (Particle.cpp:109-128), no fused multiply-adds ----
+                const float m = ip.x;
+                float vx = v.x, vy = v.y, vz = v.z;
+                if (m > 0.0f)
+                {
+                    vx = __fadd_rn(vx, __fmul_rn(__fdiv_rn(fx, m), p.dt));
+                    vy = __fadd_rn(vy, __fmul_rn(__fdiv_rn(fy, m), p.dt));
+                    vz = __fadd_rn(vz, __fmul_rn(__fdiv_rn(fz, m), p.dt));
+                }
+                const float v2 = vx * vx + vy * vy + vz * vz;
+                e[5] = 0.5f * m * v2 * p.k_kin;
+                const float nx = __fadd_rn(pi.x, __fmul_rn(vx, p.dt));
+                const float ny = __fadd_rn(pi.y, __fmul_rn(vy, p.dt));
+                const float nz = __fadd_rn(pi.z, __fmul_rn(vz, p.dt));
+                p.pos[sb ^ 1][s] = make_float4(nx, ny, nz, pi.w);
+                p.vel[sb ^ 1][s] = make_float4(vx, vy, vz, 0.f);
+                if (!isfinite(nx) || !isfinite(ny) || !isfinite(nz))
+                    pend |= ST_NONFINITE;
+                const float4 b = p.pos_build[s];
+                const float ddx = nx - b.x, ddy = ny - b.y, ddz = nz - b.z;
+                if (ddx * ddx + ddy * ddy + ddz * ddz > p.half_skin2)
+                    pend |= ST_STALE;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        eacc[k] += e[k];
+    return pend;
+}
+
+} // namespace
+} // namespace bsg

@@ -51,4 +51,18 @@ int launch_diag_pairs(const Params &p, int term, long long *out, unsigned long l
                       unsigned long long cap, cudaStream_t stream);
 int launch_set_positions(const Params &p, const float *xyz, const float *vel, cudaStream_t stream);
 
+// Batched ensembles (bs_batch.cu).
+constexpr int kBatchMaxBlock = 512; // largest block of the persistent step kernel
+struct BatchShape
+{
+    int block;   // threads per block
+    int lanes;   // threads per particle (1, 2, 4, 8)
+    int cluster; // blocks per cluster (1, 2, 4, 8)
+};
+int launch_batch_grid(const Params &p, cudaStream_t stream);
+int launch_batch_pairlist(const Params &p, cudaStream_t stream);
+cudaError_t launch_batch_run(const Params &p, const BatchShape &shape, int chunk, cudaStream_t stream);
+int launch_batch_finish(const Params &p, int chunk, cudaStream_t stream);
+cudaError_t batch_max_clusters(const Params &p, const BatchShape &shape, int *out);
+
 } // namespace bsg

@@ -6,6 +6,7 @@
 // a splitmix64 stream, and the file is compiled with -ffp-contract=off, so a
 // seed gives the same coordinates on x86-64 and aarch64.
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <vector>
@@ -101,6 +102,16 @@ double bs_synth_ca_chain(int64_t n, uint64_t seed, double step, double rg_target
         bool placed = false;
         for (int attempt = 0; !placed; ++attempt)
         {
+            if (attempt >= 50000)
+            {
+                // the chain end is walled in by its own beads: start the walk again in a
+                // slightly larger ball (same random stream)
+                std::fill(grid.head.begin(), grid.head.end(), -1);
+                grid.insert(0, &pts[0]);
+                R *= 1.02;
+                i = 1;
+                attempt = 0;
+            }
             if (attempt > 0 && attempt % 200 == 0)
                 R *= 1.01;
             double d[3], len2;

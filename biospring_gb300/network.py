@@ -99,6 +99,32 @@ class SpringNetwork:
         self.config = config
         self._check(self._lib.bs_setup(self._h, C.byref(config)), self._h)
 
+    # -- batched ensembles -----------------------------------------------------------------
+    def setSystems(self, offsets):
+        """Partitions the particles into independent systems: system b owns
+        [offsets[b], offsets[b + 1]). Call before :meth:`setup`."""
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        self._check(self._lib.bs_set_systems(self._h, int(off.shape[0] - 1), ptr(off, C.c_int64)), self._h)
+        self.nsys = int(off.shape[0] - 1)
+
+    def getSystemEnergies(self) -> np.ndarray:
+        out = np.zeros((self.nsys, 6), dtype=np.float64)
+        self._check(self._lib.bs_get_system_energies(self._h, ptr(out, C.c_double)), self._h)
+        return out
+
+    def setBatchShape(self, block: int, lanes: int, cluster: int):
+        self._check(self._lib.bs_set_batch_shape(self._h, int(block), int(lanes), int(cluster)), self._h)
+
+    def batchShape(self) -> tuple:
+        out = np.zeros(3, dtype=np.int32)
+        self._check(self._lib.bs_get_batch_shape(self._h, ptr(out, C.c_int32)), self._h)
+        return tuple(int(v) for v in out)
+
+    def batchAutotune(self) -> tuple:
+        out = np.zeros(3, dtype=np.int32)
+        self._check(self._lib.bs_batch_autotune(self._h, ptr(out, C.c_int32)), self._h)
+        return tuple(int(v) for v in out)
+
     def computeStep(self, nsteps: int = 1):
         self._check(self._lib.bs_step(self._h, int(nsteps)), self._h)
 

@@ -186,3 +186,19 @@ def membrane_globule(n: int = 20_000, seed: int = 3, spring_cutoff: float = 8.0,
 def ensemble_sizes(count: int = 512, lo: int = 200, hi: int = 20_000, seed: int = 2024) -> np.ndarray:
     rng = np.random.default_rng(seed)
     return np.exp(rng.uniform(np.log(lo), np.log(hi), size=count)).astype(np.int64)
+
+
+def ensemble(sizes, seed: int = 2024, **kw) -> System:
+    """Batched ensemble: independent Calpha networks (built as ``ca_network``, one seed each)
+    concatenated into one System; ``meta["offsets"]`` (int64, len(sizes) + 1) gives each
+    system's particle range."""
+    parts = [ca_network(int(nb), seed=seed + 1000 * b + 1, **kw) for b, nb in enumerate(sizes)]
+    offsets = np.zeros(len(parts) + 1, dtype=np.int64)
+    for b, s in enumerate(parts):
+        offsets[b + 1] = offsets[b] + s.n
+    xyz = np.concatenate([s.xyz for s in parts]).astype(np.float32)
+    ij = np.concatenate([s.ij + np.int32(offsets[b]) for b, s in enumerate(parts)]).astype(np.int32)
+    r0 = np.concatenate([s.r0 for s in parts]).astype(np.float32)
+    kk = np.concatenate([s.k for s in parts]).astype(np.float32)
+    return System(f"ensemble_{len(parts)}_s{seed}", xyz, ij, r0, kk, dict(parts[0].config),
+                  meta=dict(seed=seed, offsets=offsets, systems=len(parts), springs=int(ij.shape[0])))

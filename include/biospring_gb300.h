@@ -223,6 +223,32 @@ int bs_get_launch_count(bs_sim *sim, int64_t *count);
 /* Copies the last error message of the handle (or of the library when sim is NULL). */
 int bs_last_error(bs_sim *sim, char *buf, size_t len);
 
+/* ---- batched ensembles ----------------------------------------------------------
+ *
+ * Many independent networks in one handle (no reference counterpart: the reference runs one
+ * SpringNetwork per process). Upload the systems' particles concatenated with
+ * bs_upload_particles, their springs with bs_upload_springs (indices into the concatenation;
+ * a spring may not join two systems), then declare the partition before bs_setup:
+ * system b owns particles [offsets[b], offsets[b+1]). All systems share one bs_config.
+ * bs_step advances every system by nsteps with a persistent kernel in which a
+ * thread-block cluster owns whole systems; bs_get_positions / bs_get_velocities /
+ * bs_compute_forces work on the concatenation, bs_get_energies gives the sums over systems and
+ * bs_get_system_energies each system's. External forces and the pair/cell diagnostics are for
+ * single systems (BS_E_STATE). */
+int bs_set_systems(bs_sim *sim, int32_t nsys, const int64_t *offsets);
+
+/* Energies of every system of a batch after its last step: double[nsys * BS_NUM_ENERGIES]. */
+int bs_get_system_energies(bs_sim *sim, double *out);
+
+/* Launch shape of the persistent batched step kernel: threads per block (128, 256, 512),
+ * threads per particle (1, 2, 4, 8) and blocks per cluster (1, 2, 4, 8). */
+int bs_set_batch_shape(bs_sim *sim, int32_t block, int32_t lanes, int32_t cluster);
+int bs_get_batch_shape(bs_sim *sim, int32_t shape[3]);
+
+/* Times the persistent kernel for one period of the current state under every shape (the state is
+ * restored after each trial), keeps the fastest and writes it to shape (nullable). */
+int bs_batch_autotune(bs_sim *sim, int32_t shape[3]);
+
 /* ---- nonbonded forces without allocation (no counterpart in the reference) ------
  *
  * Steric, Coulomb and hydrophobic forces and energies of at most

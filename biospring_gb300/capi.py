@@ -73,6 +73,7 @@ class BsConfig(C.Structure):
         ("impala_alpha", C.c_double),
         ("rebuild_every", C.c_int32),
         ("list_skin", C.c_double),
+        ("precise_positions", C.c_int32),
     ]
 
     def to_dict(self) -> dict:
@@ -116,6 +117,9 @@ SIGNATURES = {
     "bs_get_launch_count": (C.c_int, [C.c_void_p, _i64p]),
     "bs_last_error": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "bs_set_systems": (C.c_int, [C.c_void_p, C.c_int32, _i64p]),
+    "bs_get_spring_count": (C.c_int, [C.c_void_p, _i64p]),
+    "bs_set_spring_parameters": (C.c_int, [C.c_void_p, _f32p, _f32p]),
+    "bs_adjoint": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _f32p, _f64p, _f32p, _f32p, _f32p]),
     "bs_get_system_energies": (C.c_int, [C.c_void_p, _f64p]),
     "bs_set_batch_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "bs_get_batch_shape": (C.c_int, [C.c_void_p, _i32p]),

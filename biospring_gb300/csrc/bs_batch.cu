@@ -468,6 +468,8 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 2) k_batch_run(Params p, int c
             {
                 p.pos[to][s] = p.pos[from][s];
                 p.vel[to][s] = p.vel[from][s];
+                if (p.pos_lo[0])
+                    p.pos_lo[to][s] = p.pos_lo[from][s];
             }
         }
         cl.sync();

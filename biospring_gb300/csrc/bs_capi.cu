@@ -83,6 +83,21 @@ struct bs_sim
     BatchShape shape{256, 4, 1};
     int *cl_start_d = nullptr;
     int *cl_sys_d = nullptr;
+    // adjoint: directed spring ids of the caller-order CSR, scratch, and the captured run
+    std::vector<unsigned int> csr_sid;
+    std::vector<int> csr_pos; // CSR position of each spring's two directed entries
+    unsigned int *sp_sid_d = nullptr;
+    DeviceBuffers adj_dev;
+    int adj_ck_cap = 0, adj_seg_cap = 0;
+    float *adj_ck_xyz = nullptr, *adj_ck_vel = nullptr, *adj_ck_lo = nullptr;
+    float4 *adj_seg = nullptr, *adj_seg_lo = nullptr, *adj_lx = nullptr, *adj_lv = nullptr, *adj_nu[2] = {nullptr, nullptr};
+    float4 *adj_cx = nullptr, *adj_cv = nullptr, *adj_target = nullptr;
+    float *adj_gk = nullptr, *adj_gr0 = nullptr, *adj_ok = nullptr, *adj_or0 = nullptr;
+    double *adj_blk = nullptr, *adj_loss = nullptr;
+    unsigned int *adj_done = nullptr;
+    cudaGraphExec_t adj_graph = nullptr;
+    int adj_key[2] = {0, 0};
+    long long adj_kernels = 0;
     // diagnostics scratch
     long long *diag_out = nullptr;
     unsigned long long *diag_count = nullptr;
@@ -120,6 +135,11 @@ void destroy_graph(bs_sim *s)
         cudaGraphExecDestroy(s->period_graph);
         s->period_graph = nullptr;
     }
+    if (s->adj_graph)
+    {
+        cudaGraphExecDestroy(s->adj_graph);
+        s->adj_graph = nullptr;
+    }
 }
 
 void free_growable(bs_sim *s);
@@ -131,6 +151,10 @@ void release_device(bs_sim *s)
         cudaStreamSynchronize(s->stream);
     free_growable(s);
     s->dev.free_all();
+    s->adj_dev.free_all();
+    s->adj_ck_cap = 0;
+    s->adj_seg_cap = 0;
+    s->sp_sid_d = nullptr;
     s->diag_out = nullptr;
     s->diag_count = nullptr;
     s->diag_cap = 0;
@@ -679,6 +703,8 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     std::vector<unsigned int> col(std::max(nnz, 1));
     std::vector<float> kk(std::max(nnz, 1)), rr(std::max(nnz, 1));
     std::vector<int> fillp(row.begin(), row.end() - 1);
+    s->csr_sid.assign(std::max(nnz, 1), 0u);
+    s->csr_pos.assign(2 * s->sp_i.size(), 0);
     auto partner_code = [&](int a, int b) {
         uint32_t code = static_cast<uint32_t>(b);
         if (s->is_static[b])
@@ -694,10 +720,14 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
         col[e] = partner_code(a, b);
         kk[e] = s->sp_k[t];
         rr[e] = s->sp_r0[t];
+        s->csr_sid[e] = static_cast<unsigned int>(2 * t);
+        s->csr_pos[2 * t] = e;
         e = fillp[b]++;
         col[e] = partner_code(b, a);
         kk[e] = s->sp_k[t];
         rr[e] = s->sp_r0[t];
+        s->csr_sid[e] = static_cast<unsigned int>(2 * t + 1);
+        s->csr_pos[2 * t + 1] = e;
     }
     int maxdeg = 1;
     for (int64_t i = 0; i < n; ++i)
@@ -763,6 +793,12 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     }
     BS_CUDA(s->dev.alloc(&p.inv, n));
     BS_CUDA(s->dev.alloc(&p.pos_build, npad));
+    if (c.precise_positions)
+        for (int b = 0; b < 2; ++b)
+        {
+            BS_CUDA(s->dev.alloc(&p.pos_lo[b], npad));
+            BS_CUDA(cudaMemsetAsync(p.pos_lo[b], 0, sizeof(float4) * npad, s->stream));
+        }
     BS_CUDA(s->dev.alloc(&p.ext, n));
     BS_CUDA(s->dev.alloc(&p.force_out, n));
     int *d_row;
@@ -1586,6 +1622,278 @@ int bs_get_system_energies(bs_sim *s, double *out)
         for (int k = 0; k < BS_NUM_ENERGIES; ++k)
             out[static_cast<size_t>(b) * BS_NUM_ENERGIES + k] = e[static_cast<size_t>(b) * 8 + k];
     return BS_OK;
+}
+
+int bs_get_spring_count(bs_sim *s, int64_t *count)
+{
+    if (!s || !count)
+        return fail(s, BS_E_ARG, "bs_get_spring_count: null argument");
+    *count = static_cast<int64_t>(s->sp_i.size());
+    return BS_OK;
+}
+
+int bs_set_spring_parameters(bs_sim *s, const float *stiffness, const float *equilibrium)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    int rc = bs_synchronize(s);
+    if (rc)
+        return rc;
+    const size_t ns = s->sp_i.size();
+    if (ns == 0)
+        return BS_OK;
+    for (size_t t = 0; t < ns; ++t)
+    {
+        if (stiffness)
+            s->sp_k[t] = stiffness[t];
+        if (equilibrium)
+            s->sp_r0[t] = equilibrium[t];
+    }
+    const size_t nnz = 2 * ns;
+    std::vector<float> kk(nnz), rr(nnz);
+    for (size_t t = 0; t < ns; ++t)
+        for (int e = 0; e < 2; ++e)
+        {
+            kk[s->csr_pos[2 * t + e]] = s->sp_k[t];
+            rr[s->csr_pos[2 * t + e]] = s->sp_r0[t];
+        }
+    BS_CUDA(cudaMemcpyAsync(const_cast<float *>(s->p.sp_k), kk.data(), sizeof(float) * nnz, cudaMemcpyHostToDevice,
+                            s->stream));
+    BS_CUDA(cudaMemcpyAsync(const_cast<float *>(s->p.sp_r0), rr.data(), sizeof(float) * nnz, cudaMemcpyHostToDevice,
+                            s->stream));
+    BS_CUDA(cudaStreamSynchronize(s->stream));
+    s->list_valid = false; // the next rebuild copies them into the sorted spring table
+    return BS_OK;
+}
+
+// Records the whole adjoint run (forward with checkpoints, then the backward sweep with
+// recomputation from each checkpoint) on the handle's stream.
+static int record_adjoint(bs_sim *s, int nsteps, int K)
+{
+    Params &p = s->p;
+    const int S = (nsteps + K - 1) / K;
+    const size_t n3 = 3 * static_cast<size_t>(s->n), np = static_cast<size_t>(p.npad);
+    auto seg_len = [&](int seg) { return std::min(K, nsteps - seg * K); };
+    float4 *lo_seg = p.pos_lo[0] ? s->adj_seg_lo : nullptr;
+    BS_CUDA(cudaMemsetAsync(s->adj_gk, 0, sizeof(float) * 2 * std::max<size_t>(s->sp_i.size(), 1), s->stream));
+    BS_CUDA(cudaMemsetAsync(s->adj_gr0, 0, sizeof(float) * 2 * std::max<size_t>(s->sp_i.size(), 1), s->stream));
+    // forward: a checkpoint (caller order) and a rebuild at the start of every interval; the
+    // positions of the last interval are kept as they are produced
+    for (int seg = 0; seg < S; ++seg)
+    {
+        s->launches += launch_unsort(p, 0, s->adj_ck_xyz + seg * n3, s->stream);
+        s->launches += launch_unsort(p, 1, s->adj_ck_vel + seg * n3, s->stream);
+        if (p.pos_lo[0])
+            s->launches += launch_unsort(p, 3, s->adj_ck_lo + seg * n3, s->stream);
+        s->launches += launch_rebuild(p, s->stream);
+        for (int k = 0; k < seg_len(seg); ++k)
+        {
+            if (seg == S - 1)
+                s->launches += launch_adj_save(p, s->adj_seg + k * np, lo_seg ? lo_seg + k * np : nullptr, s->stream);
+            s->launches += launch_step(p, MODE_STEP, s->stream);
+        }
+    }
+    AdjState a{nullptr, nullptr, s->adj_lx, s->adj_lv, s->adj_nu[0], s->adj_nu[1], s->adj_gk, s->adj_gr0};
+    s->launches += launch_adj_init(p, a, s->adj_target, s->adj_blk, s->adj_done, s->adj_loss, s->stream);
+    int cur = 0;
+    for (int seg = S - 1; seg >= 0; --seg)
+    {
+        const int len = seg_len(seg);
+        if (seg != S - 1)
+        {
+            a.nu_in = s->adj_nu[cur];
+            s->launches += launch_adj_permute(p, a, s->adj_cx, s->adj_cv, 0, s->stream);
+            s->launches += launch_set_positions(p, s->adj_ck_xyz + seg * n3, s->adj_ck_vel + seg * n3, s->stream,
+                                                p.pos_lo[0] ? s->adj_ck_lo + seg * n3 : nullptr);
+            s->launches += launch_rebuild(p, s->stream);
+            for (int k = 0; k < len; ++k)
+            {
+                s->launches += launch_adj_save(p, s->adj_seg + k * np, lo_seg ? lo_seg + k * np : nullptr,
+                                               s->stream);
+                if (k < len - 1)
+                    s->launches += launch_step(p, MODE_STEP, s->stream);
+            }
+            s->launches += launch_adj_permute(p, a, s->adj_cx, s->adj_cv, 1, s->stream);
+        }
+        for (int k = len - 1; k >= 0; --k)
+        {
+            a.x = s->adj_seg + k * np;
+            a.xlo = lo_seg ? lo_seg + k * np : nullptr;
+            a.nu_in = s->adj_nu[cur];
+            a.nu_out = s->adj_nu[cur ^ 1];
+            s->launches += launch_adj_step(p, a, s->stream);
+            cur ^= 1;
+        }
+    }
+    s->launches += launch_adj_combine(static_cast<int>(s->sp_i.size()), s->adj_gk, s->adj_gr0, s->adj_ok, s->adj_or0,
+                                      s->stream);
+    // the state goes back to the start
+    s->launches += launch_set_positions(p, s->adj_ck_xyz, s->adj_ck_vel, s->stream,
+                                        p.pos_lo[0] ? s->adj_ck_lo : nullptr);
+    return BS_OK;
+}
+
+int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *target, double *loss, float *dL_dk,
+               float *dL_dr0, float *dL_dq)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    if (s->p.nsys > 0)
+        return fail(s, BS_E_STATE, "bs_adjoint: not available for batched ensembles");
+    if (nsteps < 1 || checkpoint < 1 || !target || !loss)
+        return fail(s, BS_E_ARG, "bs_adjoint: nsteps >= 1, checkpoint >= 1, target and loss are required");
+    if (!s->sp_i.empty() && (!dL_dk || !dL_dr0))
+        return fail(s, BS_E_ARG, "bs_adjoint: dL_dk and dL_dr0 are required");
+    if (dL_dq)
+        return fail(s, BS_E_ARG, "bs_adjoint: charge gradients are not available (pass NULL)");
+    const bs_config &c = s->cfg;
+    if (c.coulomb_enable || c.hydrophobicity_enable || c.impala_enable)
+        return fail(s, BS_E_ARG, "bs_adjoint: differentiates springs, linear steric and viscosity; "
+                                 "disable coulomb, hydrophobicity and impala");
+    if (c.steric_enable && c.steric_mode != BS_STERIC_LINEAR)
+        return fail(s, BS_E_ARG, "bs_adjoint: only the linear steric mode is differentiated");
+    if (s->ext_dirty)
+        return fail(s, BS_E_STATE, "bs_adjoint: an external force is pending; step or clear it first");
+    int rc = bs_synchronize(s);
+    if (rc)
+        return rc;
+    Params &p = s->p;
+    const int K = std::min(checkpoint, nsteps);
+    const int S = (nsteps + K - 1) / K;
+    const size_t n3 = 3 * static_cast<size_t>(s->n), np = static_cast<size_t>(p.npad);
+    const size_t ns = s->sp_i.size();
+    // directed spring ids in the sorted spring table (filled by every rebuild from now on)
+    if (!p.se_sid)
+    {
+        unsigned int *d_sid = nullptr, *e_sid = nullptr;
+        BS_CUDA(s->adj_dev.alloc(&d_sid, s->csr_sid.size()));
+        BS_CUDA(s->adj_dev.alloc(&e_sid, np * p.sp_maxdeg));
+        BS_CUDA(cudaMemcpyAsync(d_sid, s->csr_sid.data(), sizeof(unsigned int) * s->csr_sid.size(),
+                                cudaMemcpyHostToDevice, s->stream));
+        p.sp_sid = d_sid;
+        p.se_sid = e_sid;
+        s->sp_sid_d = d_sid;
+        destroy_graph(s);
+    }
+    if (S > s->adj_ck_cap || K > s->adj_seg_cap || !s->adj_lx)
+    {
+        destroy_graph(s);
+        // (buffers of a smaller earlier run stay allocated until the handle is set up again)
+        s->adj_ck_cap = std::max(S, s->adj_ck_cap);
+        s->adj_seg_cap = std::max(K, s->adj_seg_cap);
+        BS_CUDA(s->dev.alloc(&s->adj_ck_xyz, s->adj_ck_cap * n3));
+        BS_CUDA(s->dev.alloc(&s->adj_ck_vel, s->adj_ck_cap * n3));
+        BS_CUDA(s->dev.alloc(&s->adj_ck_lo, s->adj_ck_cap * n3));
+        BS_CUDA(s->dev.alloc(&s->adj_seg, s->adj_seg_cap * np));
+        if (p.pos_lo[0])
+            BS_CUDA(s->dev.alloc(&s->adj_seg_lo, s->adj_seg_cap * np));
+        BS_CUDA(s->dev.alloc(&s->adj_lx, np));
+        BS_CUDA(s->dev.alloc(&s->adj_lv, np));
+        BS_CUDA(s->dev.alloc(&s->adj_nu[0], np));
+        BS_CUDA(s->dev.alloc(&s->adj_nu[1], np));
+        BS_CUDA(s->dev.alloc(&s->adj_cx, np));
+        BS_CUDA(s->dev.alloc(&s->adj_cv, np));
+        BS_CUDA(s->dev.alloc(&s->adj_target, np));
+        BS_CUDA(s->dev.alloc(&s->adj_gk, 2 * std::max<size_t>(ns, 1)));
+        BS_CUDA(s->dev.alloc(&s->adj_gr0, 2 * std::max<size_t>(ns, 1)));
+        BS_CUDA(s->dev.alloc(&s->adj_ok, std::max<size_t>(ns, 1)));
+        BS_CUDA(s->dev.alloc(&s->adj_or0, std::max<size_t>(ns, 1)));
+        BS_CUDA(s->dev.alloc(&s->adj_blk, (np + 255) / 256));
+        BS_CUDA(s->dev.alloc(&s->adj_loss, 1));
+        BS_CUDA(s->dev.alloc(&s->adj_done, 1));
+        BS_CUDA(cudaMemsetAsync(s->adj_done, 0, sizeof(unsigned int), s->stream));
+    }
+    // the target, caller order
+    {
+        std::vector<float4> tg(np, make_float4(0.f, 0.f, 0.f, 0.f));
+        for (int64_t i = 0; i < s->n; ++i)
+            tg[i] = make_float4(target[3 * i], target[3 * i + 1], target[3 * i + 2], 0.f);
+        BS_CUDA(cudaMemcpyAsync(s->adj_target, tg.data(), sizeof(float4) * np, cudaMemcpyHostToDevice, s->stream));
+        BS_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    rc = read_ctl(s);
+    if (rc)
+        return rc;
+    const Ctl saved = *s->ctl_host;
+    for (int attempt = 0; attempt < 4; ++attempt)
+    {
+        if (!s->adj_graph || s->adj_key[0] != nsteps || s->adj_key[1] != K)
+        {
+            if (s->adj_graph)
+            {
+                cudaGraphExecDestroy(s->adj_graph);
+                s->adj_graph = nullptr;
+            }
+            cudaGraph_t g = nullptr;
+            BS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            const long long before = s->launches;
+            rc = record_adjoint(s, nsteps, K);
+            const cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+            if (rc)
+            {
+                if (g)
+                    cudaGraphDestroy(g);
+                return rc;
+            }
+            if (ce != cudaSuccess)
+                return cuda_fail(s, ce, "bs_adjoint: capture");
+            const cudaError_t ie = cudaGraphInstantiate(&s->adj_graph, g, 0);
+            cudaGraphDestroy(g);
+            if (ie != cudaSuccess)
+                return cuda_fail(s, ie, "bs_adjoint: cudaGraphInstantiate");
+            s->adj_key[0] = nsteps;
+            s->adj_key[1] = K;
+            s->adj_kernels = s->launches - before;
+            s->launches = before;
+        }
+        BS_CUDA(cudaGraphLaunch(s->adj_graph, s->stream));
+        s->launches += s->adj_kernels;
+        s->list_valid = false;
+        rc = read_ctl(s);
+        if (rc)
+            return rc;
+        const Ctl &h = *s->ctl_host;
+        if (h.status & ST_NONFINITE)
+            return fail(s, BS_E_NONFINITE, "bs_adjoint: a position became non-finite");
+        if ((h.status & ST_STALE) || h.stale_events != saved.stale_events)
+        {
+            // put the counters back before reporting
+            s->ctl_host->status &= ~ST_STALE;
+            s->ctl_host->stale_events = saved.stale_events;
+            s->ctl_host->steps = saved.steps;
+            for (int k = 0; k < 8; ++k)
+                s->ctl_host->energies[k] = saved.energies[k];
+            BS_CUDA(cudaMemcpy(s->p.ctl, s->ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice));
+            return fail(s, BS_E_CAPACITY, "bs_adjoint: a particle moved more than half the list skin within a "
+                                          "checkpoint interval; raise cuda.listskin or shorten the interval");
+        }
+        if (h.status & (ST_CELL_CAPACITY | ST_PAIR_CAPACITY | ST_WIDE))
+        {
+            // a list or the grid overflowed at one of the rebuilds: grow it (this rebuilds from the
+            // restored start state) and run again
+            rc = rebuild_now(s);
+            if (rc)
+                return rc;
+            continue;
+        }
+        // step count and energies as before the call
+        s->ctl_host->steps = saved.steps;
+        for (int k = 0; k < 8; ++k)
+            s->ctl_host->energies[k] = saved.energies[k];
+        BS_CUDA(cudaMemcpy(s->p.ctl, s->ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice));
+        BS_CUDA(cudaMemcpy(loss, s->adj_loss, sizeof(double), cudaMemcpyDeviceToHost));
+        if (ns)
+        {
+            BS_CUDA(cudaMemcpy(dL_dk, s->adj_ok, sizeof(float) * ns, cudaMemcpyDeviceToHost));
+            BS_CUDA(cudaMemcpy(dL_dr0, s->adj_or0, sizeof(float) * ns, cudaMemcpyDeviceToHost));
+        }
+        return BS_OK;
+    }
+    return fail(s, BS_E_CAPACITY, "bs_adjoint: lists did not fit after repeated growth");
 }
 
 int bs_get_launch_count(bs_sim *s, int64_t *count)

@@ -86,6 +86,7 @@ struct Ctl
     long long nominal;         // steps every system should have completed after the queued work
     int lagging;               // live systems behind `nominal` (stopped early by a stale list)
     int dead;                  // systems with a non-finite position
+    int stale_events;          // rebuilds that found a stale list (counted, never reset)
 };
 
 // Search grid of one system of a batched ensemble (same formula as the single-system grid).
@@ -117,6 +118,7 @@ struct Params
     // per-particle parameters flip at every rebuild (Ctl::lbuf)
     float4 *pos[2];           // x, y, z, steric factor P (F6 for LJ modes, radius for linear)
     float4 *vel[2];           // vx, vy, vz, 0
+    float4 *pos_lo[2];        // rounding remainders of x, y, z (precise_positions), else null
     float *fhi[2];            // second steric factor (F12 Amber, F8 Lewitt/Zacharias)
     float *chg[2];            // charge
     float *hyd[2];            // hydrophobicity
@@ -139,6 +141,9 @@ struct Params
     float *se_k;
     float *se_r0;
     int *se_deg;              // [npad]
+    // spring ids of the directed entries (2 * spring + end), for the adjoint; null when unused
+    const unsigned int *sp_sid; // caller-order CSR
+    unsigned int *se_sid;       // sorted-space ELL
     // nonbonded pair lists
     PairList pl[kLists];
     int pl16;                 // list 0 holds 16-bit offsets

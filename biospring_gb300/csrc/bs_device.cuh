@@ -504,6 +504,8 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             {
                 p.pos[sb ^ 1][s] = pi;
                 p.vel[sb ^ 1][s] = p.vel[sb][s];
+                if (p.pos_lo[0])
+                    p.pos_lo[sb ^ 1][s] = p.pos_lo[sb][s];
             }
             else
                 p.force_out[p.perm[lb][s]] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -562,9 +564,27 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
                 }
                 const float v2 = vx * vx + vy * vy + vz * vz;
                 e[5] = 0.5f * m * v2 * p.k_kin;
-                const float nx = __fadd_rn(pi.x, __fmul_rn(vx, p.dt));
-                const float ny = __fadd_rn(pi.y, __fmul_rn(vy, p.dt));
-                const float nz = __fadd_rn(pi.z, __fmul_rn(vz, p.dt));
+                float nx, ny, nz;
+                if (p.pos_lo[0])
+                {
+                    // x += v dt in float-float: the increment's rounding error and the carried
+                    // remainder are kept, so increments below half an ulp of x are not lost
+                    const float4 lo = p.pos_lo[sb][s];
+                    float ex, ey, ez;
+                    two_sum(pi.x, __fmul_rn(vx, p.dt), nx, ex);
+                    two_sum(pi.y, __fmul_rn(vy, p.dt), ny, ey);
+                    two_sum(pi.z, __fmul_rn(vz, p.dt), nz, ez);
+                    two_sum(nx, __fadd_rn(ex, lo.x), nx, ex);
+                    two_sum(ny, __fadd_rn(ey, lo.y), ny, ey);
+                    two_sum(nz, __fadd_rn(ez, lo.z), nz, ez);
+                    p.pos_lo[sb ^ 1][s] = make_float4(ex, ey, ez, 0.f);
+                }
+                else
+                {
+                    nx = __fadd_rn(pi.x, __fmul_rn(vx, p.dt));
+                    ny = __fadd_rn(pi.y, __fmul_rn(vy, p.dt));
+                    nz = __fadd_rn(pi.z, __fmul_rn(vz, p.dt));
+                }
                 p.pos[sb ^ 1][s] = make_float4(nx, ny, nz, pi.w);
                 p.vel[sb ^ 1][s] = make_float4(vx, vy, vz, 0.f);
                 if (!isfinite(nx) || !isfinite(ny) || !isfinite(nz))

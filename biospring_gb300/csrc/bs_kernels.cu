@@ -118,6 +118,8 @@ __global__ void __launch_bounds__(kBboxBlock) k_bbox(Params p)
         ctl->ncells_needed = cells < 2.0e9 ? static_cast<int>(cells) : INT_MAX;
         atomicOr(&ctl->status, ST_CELL_CAPACITY);
     }
+    if (status_of(ctl) & ST_STALE)
+        ctl->stale_events += 1;
     atomicAnd(&ctl->status, ~ST_STALE);
     ctl->done_bbox = 0u;
 }
@@ -233,6 +235,8 @@ __global__ void __launch_bounds__(kBuildBlock) k_reorder(Params p)
         const float4 q = p.pos[sb][old];
         p.pos[sb ^ 1][i] = q;
         p.vel[sb ^ 1][i] = p.vel[sb][old];
+        if (p.pos_lo[0])
+            p.pos_lo[sb ^ 1][i] = p.pos_lo[sb][old];
         p.fhi[lb ^ 1][i] = p.fhi[lb][old];
         p.chg[lb ^ 1][i] = p.chg[lb][old];
         p.hyd[lb ^ 1][i] = p.hyd[lb][old];
@@ -280,6 +284,8 @@ __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
         p.se_col[dst] = slot | (c & ~kSlotMask);
         p.se_k[dst] = p.sp_k[e];
         p.se_r0[dst] = p.sp_r0[e];
+        if (p.se_sid)
+            p.se_sid[dst] = p.sp_sid[e];
     }
     p.se_deg[s] = r1 - r0;
 }
@@ -561,8 +567,8 @@ __global__ void __launch_bounds__(kStepBlock, kStepMinBlocks) k_step(Params p)
 // Host-facing helpers
 // ------------------------------------------------------------------------------------------
 
-// Writes positions (what = 0), velocities (1) or forces of the last force-only evaluation (2)
-// in caller order as float[3n].
+// Writes positions (what = 0), velocities (1), forces of the last force-only evaluation (2) or
+// the positions' rounding remainders (3, precise_positions) in caller order as float[3n].
 __global__ void k_unsort(Params p, int what, float *out)
 {
     const Ctl *ctl = p.ctl;
@@ -578,14 +584,19 @@ __global__ void k_unsort(Params p, int what, float *out)
         return;
     }
     const int id = p.perm[ctl->lbuf][s];
-    const float4 q = what == 0 ? p.pos[ctl->sbuf][s] : p.vel[ctl->sbuf][s];
+    float4 q;
+    if (what == 3)
+        q = p.pos_lo[0] ? p.pos_lo[ctl->sbuf][s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    else
+        q = what == 0 ? p.pos[ctl->sbuf][s] : p.vel[ctl->sbuf][s];
     out[3 * id] = q.x;
     out[3 * id + 1] = q.y;
     out[3 * id + 2] = q.z;
 }
 
-// Overwrites positions and/or velocities from caller-order float[3n] arrays (nullable).
-__global__ void k_set_state(Params p, const float *xyz, const float *vel)
+// Overwrites positions and/or velocities from caller-order float[3n] arrays (nullable); new
+// positions get the rounding remainders `lo` (float[3n], nullable: zero).
+__global__ void k_set_state(Params p, const float *xyz, const float *vel, const float *lo)
 {
     const Ctl *ctl = p.ctl;
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
@@ -599,6 +610,9 @@ __global__ void k_set_state(Params p, const float *xyz, const float *vel)
         q.y = xyz[3 * id + 1];
         q.z = xyz[3 * id + 2];
         p.pos[ctl->sbuf][s] = q;
+        if (p.pos_lo[0])
+            p.pos_lo[ctl->sbuf][s] = lo ? make_float4(lo[3 * id], lo[3 * id + 1], lo[3 * id + 2], 0.f)
+                                        : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     if (vel)
         p.vel[ctl->sbuf][s] = make_float4(vel[3 * id], vel[3 * id + 1], vel[3 * id + 2], 0.f);
@@ -823,9 +837,9 @@ int launch_unsort(const Params &p, int what, float *out3, cudaStream_t st)
     return 1;
 }
 
-int launch_set_positions(const Params &p, const float *xyz, const float *vel, cudaStream_t st)
+int launch_set_positions(const Params &p, const float *xyz, const float *vel, cudaStream_t st, const float *lo)
 {
-    k_set_state<<<(p.n + 255) / 256, 256, 0, st>>>(p, xyz, vel);
+    k_set_state<<<(p.n + 255) / 256, 256, 0, st>>>(p, xyz, vel, lo);
     return 1;
 }
 

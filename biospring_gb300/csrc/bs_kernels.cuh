@@ -49,7 +49,27 @@ int launch_diag_cells(const Params &p, float cutoff, float skin, uint32_t need_f
                       cudaStream_t stream);
 int launch_diag_pairs(const Params &p, int term, long long *out, unsigned long long *count,
                       unsigned long long cap, cudaStream_t stream);
-int launch_set_positions(const Params &p, const float *xyz, const float *vel, cudaStream_t stream);
+int launch_set_positions(const Params &p, const float *xyz, const float *vel, cudaStream_t stream,
+                         const float *lo = nullptr);
+
+// Discrete adjoint (bs_adjoint.cu).
+struct AdjState
+{
+    const float4 *x;   // positions at the start of the step being reversed (sorted layout)
+    const float4 *xlo; // their rounding remainders (precise_positions), else null
+    float4 *lx;      // dL/dx
+    float4 *lv;      // dL/dv
+    float4 *nu_in;   // b (lambda_v + dt lambda_x) of the later step
+    float4 *nu_out;  // the same for the step being reversed
+    float *gk;       // per directed spring entry: dL/dk, dL/dr0 partial sums
+    float *gr0;
+};
+int launch_adj_step(const Params &p, const AdjState &a, cudaStream_t stream);
+int launch_adj_init(const Params &p, const AdjState &a, const float4 *target, double *blk, unsigned int *done,
+                    double *loss, cudaStream_t stream);
+int launch_adj_permute(const Params &p, const AdjState &a, float4 *cx, float4 *cv, int dir, cudaStream_t stream);
+int launch_adj_save(const Params &p, float4 *dst, float4 *dst_lo, cudaStream_t stream);
+int launch_adj_combine(int nsp, const float *gk, const float *gr0, float *ok, float *or0, cudaStream_t stream);
 
 // Batched ensembles (bs_batch.cu).
 constexpr int kBatchMaxBlock = 512; // largest block of the persistent step kernel

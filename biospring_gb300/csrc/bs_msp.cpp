@@ -95,7 +95,7 @@ const std::set<std::string> &known_names()
                       "charge"});
         add("rigidbody", {"enable", "enablesampling", "enablemontecarlo", "montecarlo_translation_norm",
                           "montecarlo_rotation_norm", "montecarlo_temperature"});
-        add("cuda", {"dielectricmode", "rebuildevery", "listskin", "impalaz0", "impalaalpha"});
+        add("cuda", {"dielectricmode", "rebuildevery", "listskin", "impalaz0", "impalaalpha", "precisepositions"});
         return n;
     }();
     return names;
@@ -142,7 +142,7 @@ extern "C" int bs_config_parse_msp(const char *text, bs_config *cfg, char *err, 
         double d = 0.0;
         int32_t b = 0;
         if (param == "enable" || param == "enableelectrostatic" || param == "enablesteric" ||
-            param == "enablesampling" || param == "enablemontecarlo")
+            param == "enablesampling" || param == "enablemontecarlo" || name == "cuda.precisepositions")
         {
             ok = parse_bool(value, b);
             if (!ok)
@@ -162,6 +162,8 @@ extern "C" int bs_config_parse_msp(const char *text, bs_config *cfg, char *err, 
                 c.viscosity_enable = b;
             else if (group == "rigidbody" && param == "enable")
                 c.rigidbody_enable = b;
+            else if (name == "cuda.precisepositions")
+                c.precise_positions = b;
         }
         else if (name == "steric.mode")
         {

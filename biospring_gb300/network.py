@@ -99,6 +99,29 @@ class SpringNetwork:
         self.config = config
         self._check(self._lib.bs_setup(self._h, C.byref(config)), self._h)
 
+    # -- gradients ---------------------------------------------------------------------------
+    def springCount(self) -> int:
+        c = C.c_int64()
+        self._check(self._lib.bs_get_spring_count(self._h, C.byref(c)), self._h)
+        return c.value
+
+    def setSpringParameters(self, stiffness=None, equilibrium=None):
+        k = _f32(stiffness)
+        r0 = _f32(equilibrium)
+        self._check(self._lib.bs_set_spring_parameters(self._h, ptr(k, C.c_float), ptr(r0, C.c_float)), self._h)
+
+    def adjoint(self, nsteps: int, target, checkpoint: int = 20):
+        """Loss (1/n) sum |x(nsteps) - target|^2 and its gradient with respect to every spring's
+        stiffness and rest length, by the discrete adjoint (the state is left unchanged)."""
+        tg = _f32(target, (-1, 3))
+        ns = self.springCount()
+        gk = np.zeros(max(ns, 1), dtype=np.float32)
+        gr = np.zeros(max(ns, 1), dtype=np.float32)
+        loss = C.c_double()
+        self._check(self._lib.bs_adjoint(self._h, int(nsteps), int(checkpoint), ptr(tg, C.c_float), C.byref(loss),
+                                         ptr(gk, C.c_float), ptr(gr, C.c_float), None), self._h)
+        return loss.value, gk[:ns], gr[:ns]
+
     # -- batched ensembles -----------------------------------------------------------------
     def setSystems(self, offsets):
         """Partitions the particles into independent systems: system b owns

@@ -202,3 +202,30 @@ def ensemble(sizes, seed: int = 2024, **kw) -> System:
     kk = np.concatenate([s.k for s in parts]).astype(np.float32)
     return System(f"ensemble_{len(parts)}_s{seed}", xyz, ij, r0, kk, dict(parts[0].config),
                   meta=dict(seed=seed, offsets=offsets, systems=len(parts), springs=int(ij.shape[0])))
+
+
+def smooth_displacement(xyz: np.ndarray, seed: int, amplitude: float = 2.0, modes: int = 3) -> np.ndarray:
+    """A seeded smooth displacement field: a sum of `modes` low-wavenumber sinusoids per axis with
+    seeded directions and phases, scaled so that max |u| = amplitude (A)."""
+    rng = np.random.default_rng(seed)
+    x = xyz.astype(np.float64)
+    span = max(float(np.ptp(x, axis=0).max()), 1.0)
+    u = np.zeros_like(x)
+    for _ in range(modes):
+        kvec = rng.normal(size=3)
+        kvec *= (2.0 * np.pi / span) / np.linalg.norm(kvec)
+        phase = rng.uniform(0.0, 2.0 * np.pi, size=3)
+        amp = rng.normal(size=3)
+        u += amp[None, :] * np.sin(x @ kvec[:, None] + phase[None, :])
+    u *= amplitude / np.sqrt((u * u).sum(axis=1)).max()
+    return u
+
+
+def adjoint_fit(n: int = 10_000, seed: int = 4, amplitude: float = 2.0, nsteps: int = 200) -> tuple:
+    """The adjoint workload: a Calpha network built as ``ca_network`` and a target equal to the
+    start positions plus a seeded smooth displacement field of the given amplitude. Returns
+    (System, target float32 (n, 3), nsteps)."""
+    s = ca_network(n, seed=seed)
+    target = (s.xyz.astype(np.float64) + smooth_displacement(s.xyz, seed + 17, amplitude)).astype(np.float32)
+    s.meta["nsteps"] = nsteps
+    return s, target, nsteps

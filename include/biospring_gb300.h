@@ -103,6 +103,8 @@ typedef struct bs_config {
     double impala_alpha;      /* reference hard-codes 1.99 */
     int32_t rebuild_every;    /* rebuild the device pair list every K steps (>= 1) */
     double list_skin;         /* A; extra radius of the device pair list; drift > skin/2 forces a rebuild */
+    int32_t precise_positions; /* carry each position's rounding remainder (float-float x += v dt);
+                                  off (0) reproduces the reference's FP32 update */
 } bs_config;
 
 typedef struct bs_sim bs_sim;
@@ -222,6 +224,27 @@ int bs_get_launch_count(bs_sim *sim, int64_t *count);
 
 /* Copies the last error message of the handle (or of the library when sim is NULL). */
 int bs_last_error(bs_sim *sim, char *buf, size_t len);
+
+/* ---- gradients (no counterpart in the reference) ----------------------------------
+ *
+ * Number of springs the handle holds (bs_upload_springs ignores repeated pairs); the spring
+ * arrays below have this length, in upload order. */
+int bs_get_spring_count(bs_sim *sim, int64_t *count);
+
+/* Replaces every spring's stiffness and/or rest length (nullable arrays keep the current
+ * values), e.g. between steps of a parameter fit. Takes effect at the next step. */
+int bs_set_spring_parameters(bs_sim *sim, const float *stiffness, const float *equilibrium);
+
+/* Loss L = (1/n) sum_i |x_i(nsteps) - target_i|^2 after nsteps steps from the current state, and
+ * its gradient with respect to every spring's stiffness (dL_dk) and rest length (dL_dr0), by the
+ * discrete adjoint of the damped step with checkpoints every `checkpoint` steps and
+ * recomputation in between (FP32 adjoint state). The steps run with a rebuild at every
+ * checkpoint; the state, step count and energies are left as they were. Differentiates springs,
+ * the linear steric mode and viscosity: Coulomb, hydrophobic and IMPALA terms are BS_E_ARG, and
+ * so is a non-NULL dL_dq (charge gradients are not available). A particle that moves more than
+ * half the list skin within one checkpoint interval gives BS_E_CAPACITY. target is float[3n]. */
+int bs_adjoint(bs_sim *sim, int32_t nsteps, int32_t checkpoint, const float *target, double *loss,
+               float *dL_dk, float *dL_dr0, float *dL_dq);
 
 /* ---- batched ensembles ----------------------------------------------------------
  *

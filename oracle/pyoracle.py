@@ -23,11 +23,11 @@ REF_SO = os.path.join(HERE, "_ref", "libbsref.so")
 
 
 def build_oracle() -> str:
-    src = os.path.join(HERE, "bs_oracle.cpp")
+    srcs = [os.path.join(HERE, "bs_oracle.cpp"), os.path.join(HERE, "adjoint_fp64.cpp")]
     hdr = os.path.join(os.path.dirname(HERE), "include", "biospring_gb300.h")
-    if (not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < max(os.path.getmtime(src),
-                                                                           os.path.getmtime(hdr))):
-        subprocess.run(["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", src,
+    if (not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < max([os.path.getmtime(f) for f in srcs] +
+                                                                           [os.path.getmtime(hdr)])):
+        subprocess.run(["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", *srcs,
                         "-o", ORACLE_SO], check=True)
     return ORACLE_SO
 
@@ -209,3 +209,68 @@ class Oracle(_CpuSim):
 class Reference(_CpuSim):
     PREFIX = "bsref_"
     PATH = REF_SO
+
+
+# ---- FP64 gradient reference (adjoint_fp64.cpp) ------------------------------------------
+
+_ADJ = None
+
+
+def _adj_lib():
+    global _ADJ
+    if _ADJ is None:
+        lib = C.CDLL(ORACLE_SO)
+        common = [C.c_int64, _f32p, _f32p, _f32p, _f32p, _u8p, C.c_int64, _i32p, _f32p, _f32p, C.c_double, C.c_int,
+                  C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_int32, _f32p]
+        lib.bso_loss_fp64.restype = C.c_double
+        lib.bso_loss_fp64.argtypes = common
+        lib.bso_adjoint_fp64.restype = C.c_int
+        lib.bso_adjoint_fp64.argtypes = common + [_f64p, _f64p, _f64p]
+        lib.bso_fd_fp64.restype = C.c_int
+        lib.bso_fd_fp64.argtypes = common + [C.c_int64, _i64p, C.c_double, _f64p, _f64p]
+        _ADJ = lib
+    return _ADJ
+
+
+def _adj_args(system, nsteps, target):
+    cfg = system.bs_config()
+    a = system.arrays()
+    f32 = lambda v: None if v is None else np.ascontiguousarray(v, np.float32)  # noqa: E731
+    keep = dict(xyz=f32(a["xyz"]).reshape(-1), vel=f32(a["vel"]), mass=f32(a["mass"]), radius=f32(a["radius"]),
+                st=None if a["is_static"] is None else np.ascontiguousarray(a["is_static"], np.uint8),
+                ij=np.ascontiguousarray(system.ij, np.int32), k=f32(system.k), r0=f32(system.r0),
+                target=f32(target).reshape(-1))
+    args = [system.n, _p(keep["xyz"], C.c_float), _p(keep["vel"], C.c_float), _p(keep["mass"], C.c_float),
+            _p(keep["radius"], C.c_float), _p(keep["st"], C.c_uint8), int(system.ij.shape[0]),
+            _p(keep["ij"], C.c_int32), _p(keep["k"], C.c_float), _p(keep["r0"], C.c_float), float(cfg.timestep),
+            int(cfg.spring_enable), float(cfg.spring_scale), int(cfg.steric_enable), float(cfg.steric_cutoff),
+            float(cfg.steric_gridscale), int(cfg.viscosity_enable), float(cfg.viscosity_value), int(nsteps),
+            _p(keep["target"], C.c_float)]
+    return args, keep
+
+
+def loss_fp64(system, nsteps: int, target) -> float:
+    """L = (1/n) sum |x(nsteps) - target|^2 of the FP64 restated dynamics."""
+    args, _keep = _adj_args(system, nsteps, target)
+    return float(_adj_lib().bso_loss_fp64(*args))
+
+
+def adjoint_fp64(system, nsteps: int, target):
+    """(L, dL/dk, dL/dr0) by the FP64 discrete adjoint; one entry per distinct spring."""
+    args, _keep = _adj_args(system, nsteps, target)
+    ns = system.ij.shape[0]
+    gk = np.zeros(max(ns, 1), np.float64)
+    gr = np.zeros(max(ns, 1), np.float64)
+    loss = C.c_double()
+    _adj_lib().bso_adjoint_fp64(*args, C.byref(loss), _p(gk, C.c_double), _p(gr, C.c_double))
+    return loss.value, gk[:ns], gr[:ns]
+
+
+def fd_fp64(system, nsteps: int, target, springs, h: float = 1e-4):
+    """Central finite differences of the FP64 loss with respect to k and r0 of the given springs."""
+    args, _keep = _adj_args(system, nsteps, target)
+    sel = np.ascontiguousarray(springs, np.int64)
+    fk = np.zeros(sel.shape[0], np.float64)
+    fr = np.zeros(sel.shape[0], np.float64)
+    _adj_lib().bso_fd_fp64(*args, sel.shape[0], _p(sel, C.c_int64), float(h), _p(fk, C.c_double), _p(fr, C.c_double))
+    return fk, fr

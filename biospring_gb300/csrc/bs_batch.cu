@@ -195,12 +195,14 @@ __global__ void __launch_bounds__(1024) k_batch_cell_scan(Params p)
         p.cell_start[c1] = p.sys_start[b + 1];
 }
 
-// Typed pair lists of a batched ensemble: the rules of the single-system build (every pair within
-// the list radius of its term, the slot itself and spring partners excluded, static partners of the
-// steric term apart), one warp per home particle walking the (2 kGridDiv + 1)^2 contiguous
-// x-runs of its system's neighbour cells, 32 candidates per pass; a ballot appends the accepted
-// ones to the row in ascending slot order.
-template <bool PL16>
+// Typed pair lists, one warp per home particle: the rules of the cell-block build (every pair
+// within the list radius of its term, the slot itself and spring partners excluded, static
+// partners of the steric term apart); the warp walks the (2 kGridDiv + 1)^2 contiguous x-runs of
+// the neighbour cells, 32 candidates per pass, and a ballot appends the accepted ones to the row
+// in ascending slot order. Used for batched ensembles (BATCH: each system's own grid) and for
+// sparse single systems (a few particles per cell or fewer), where one block per cell would
+// mostly schedule empty blocks.
+template <bool PL16, bool BATCH>
 __global__ void __launch_bounds__(kBatchPlWarps * 32) k_batch_pairlist(Params p)
 {
     __shared__ int sh_part[kBatchPlWarps][kPlMaxDeg];
@@ -236,9 +238,15 @@ __global__ void __launch_bounds__(kBatchPlWarps * 32) k_batch_pairlist(Params p)
         if (on0 || on1 || on2)
         {
             const float4 pi = pos[i];
-            const int b = p.sys_of[i];
-            const int cbase = p.sys_cells[b];
-            const int nx = p.sys_grid[b].nx, ny = p.sys_grid[b].ny, nz = p.sys_grid[b].nz;
+            int cbase = 0, nx = ctl->gnx, ny = ctl->gny, nz = ctl->gnz;
+            if (BATCH)
+            {
+                const int b = p.sys_of[i];
+                cbase = p.sys_cells[b];
+                nx = p.sys_grid[b].nx;
+                ny = p.sys_grid[b].ny;
+                nz = p.sys_grid[b].nz;
+            }
             const int lc = p.cell_of[i] - cbase;
             const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
             // spring partners of i, sorted ascending in shared memory (rank sort across the warp)
@@ -554,10 +562,17 @@ int launch_batch_pairlist(const Params &p, cudaStream_t st)
         blocks = 152 * 64;
     if (blocks < 1)
         blocks = 1;
-    if (p.pl16)
-        k_batch_pairlist<true><<<static_cast<int>(blocks), kBatchPlWarps * 32, 0, st>>>(p);
+    if (p.nsys > 0)
+    {
+        if (p.pl16)
+            k_batch_pairlist<true, true><<<static_cast<int>(blocks), kBatchPlWarps * 32, 0, st>>>(p);
+        else
+            k_batch_pairlist<false, true><<<static_cast<int>(blocks), kBatchPlWarps * 32, 0, st>>>(p);
+    }
+    else if (p.pl16)
+        k_batch_pairlist<true, false><<<static_cast<int>(blocks), kBatchPlWarps * 32, 0, st>>>(p);
     else
-        k_batch_pairlist<false><<<static_cast<int>(blocks), kBatchPlWarps * 32, 0, st>>>(p);
+        k_batch_pairlist<false, false><<<static_cast<int>(blocks), kBatchPlWarps * 32, 0, st>>>(p);
     return 1;
 }
 

@@ -77,7 +77,7 @@ struct bs_sim
     long long launches = 0;
     // growable buffers (pair lists, grid arrays), freed on regrowth
     unsigned int *pl_idx[kLists] = {nullptr, nullptr, nullptr, nullptr};
-    int *cell_buf[3] = {nullptr, nullptr, nullptr};
+    int *cell_buf[4] = {nullptr, nullptr, nullptr, nullptr};
     // batched ensembles: caller's partition into systems (empty: one system)
     std::vector<int64_t> sys_off;
     BatchShape shape{256, 4, 1};
@@ -201,7 +201,7 @@ void free_growable(bs_sim *s)
             cudaFree(s->pl_idx[t]);
         s->pl_idx[t] = nullptr;
     }
-    for (int k = 0; k < 3; ++k)
+    for (int k = 0; k < 4; ++k)
     {
         if (s->cell_buf[k])
             cudaFree(s->cell_buf[k]);
@@ -227,9 +227,12 @@ int alloc_lists(bs_sim *s, const int caps[kLists], int cell_cap)
     for (int k = 0; k < 3; ++k)
         BS_CUDA(cudaMalloc(reinterpret_cast<void **>(&s->cell_buf[k]), (static_cast<size_t>(cell_cap) + 1) * sizeof(int)));
     BS_CUDA(cudaMemsetAsync(s->cell_buf[0], 0, (static_cast<size_t>(cell_cap) + 1) * sizeof(int), s->stream));
+    BS_CUDA(cudaMalloc(reinterpret_cast<void **>(&s->cell_buf[3]),
+                       (static_cast<size_t>(cell_cap) / kScanTile + 2) * sizeof(int)));
     p.cell_cnt = s->cell_buf[0];
     p.cell_start = s->cell_buf[1];
     p.cell_fill = s->cell_buf[2];
+    p.tile_sum = s->cell_buf[3];
     p.cell_cap = cell_cap;
     destroy_graph(s);
     return BS_OK;
@@ -870,6 +873,9 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
         density = std::max(density, static_cast<double>(i1 - i0) / volume);
     }
     const int cell_cap = static_cast<int>(std::min(2.0 * cells + 1024.0, 2.0e8));
+    // fewer than ~8 particles per cell: one warp per particle builds the lists faster than one
+    // block per (mostly empty) cell
+    p.pl_sparse = static_cast<double>(n) < 8.0 * cells ? 1 : 0;
     // first capacity: 1.5x the mean count expected in the list sphere, at least 32
     int caps[kLists];
     for (int t = 0; t < kLists; ++t)

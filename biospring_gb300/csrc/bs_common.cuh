@@ -154,6 +154,8 @@ struct Params
     int *cell_fill;           // [cell_cap]
     int *tmp_perm;            // [npad]
     int cell_cap;
+    int *tile_sum;            // [cell_cap / kScanTile + 2] per-tile totals of the cell scan
+    int pl_sparse;            // build the pair lists one warp per particle (few particles per cell)
     // energies: per-block partials
     double *blk_energy;       // [step blocks * 8]
     Ctl *ctl;

@@ -143,19 +143,78 @@ __global__ void __launch_bounds__(kBuildBlock) k_cell_count(Params p)
     atomicAdd(&p.cell_cnt[c], 1);
 }
 
-// Single-block exclusive scan of the cell counts; also primes the fill cursors and
-// clears the counts for the next rebuild.
-__global__ void __launch_bounds__(1024) k_cell_scan(Params p)
+// Exclusive scan of the cell counts in three passes over tiles of kScanTile cells, so that grids
+// of millions of (mostly empty) cells cost a few microseconds. Pass 1: each block scans one tile
+// (4 consecutive cells per thread) and writes the in-tile prefixes and the tile's total.
+__global__ void __launch_bounds__(1024) k_scan_tiles(Params p)
 {
     Ctl *ctl = p.ctl;
     if (status_of(ctl) & kRebuildBlocking)
         return;
     const int nc = ctl->gnx * ctl->gny * ctl->gnz;
-    const int per = (nc + blockDim.x - 1) / blockDim.x;
-    const int b0 = threadIdx.x * per, b1 = min(nc, b0 + per);
+    const int base = blockIdx.x * kScanTile;
+    if (base >= nc)
+        return;
+    const int c0 = base + 4 * threadIdx.x;
+    int v[4], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        v[k] = c0 + k < nc ? p.cell_cnt[c0 + k] : 0;
+        sum += v[k];
+    }
+    __shared__ int sh_warp[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o)
+            inc += t;
+    }
+    if (lane == 31)
+        sh_warp[warp] = inc;
+    __syncthreads();
+    if (warp == 0)
+    {
+        int w = sh_warp[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const int t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o)
+                w += t;
+        }
+        sh_warp[lane] = w; // inclusive over warps
+    }
+    __syncthreads();
+    int run = inc - sum + (warp > 0 ? sh_warp[warp - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        if (c0 + k < nc)
+            p.cell_start[c0 + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == blockDim.x - 1)
+        p.tile_sum[blockIdx.x] = sh_warp[31];
+}
+
+// Pass 2 (one block): exclusive scan of the tile totals, in place; writes the grand total after
+// the last cell.
+__global__ void __launch_bounds__(1024) k_scan_top(Params p)
+{
+    Ctl *ctl = p.ctl;
+    if (status_of(ctl) & kRebuildBlocking)
+        return;
+    const int nc = ctl->gnx * ctl->gny * ctl->gnz;
+    const int nt = (nc + kScanTile - 1) / kScanTile;
+    const int per = (nt + blockDim.x - 1) / blockDim.x;
+    const int b0 = threadIdx.x * per, b1 = min(nt, b0 + per);
     int sum = 0;
-    for (int c = b0; c < b1; ++c)
-        sum += p.cell_cnt[c];
+    for (int t = b0; t < b1; ++t)
+        sum += p.tile_sum[t];
     __shared__ int sh[1024];
     sh[threadIdx.x] = sum;
     __syncthreads();
@@ -167,16 +226,41 @@ __global__ void __launch_bounds__(1024) k_cell_scan(Params p)
         __syncthreads();
     }
     int run = sh[threadIdx.x] - sum;
-    for (int c = b0; c < b1; ++c)
+    for (int t = b0; t < b1; ++t)
     {
-        const int k = p.cell_cnt[c];
-        p.cell_start[c] = run;
-        p.cell_fill[c] = run;
-        p.cell_cnt[c] = 0;
+        const int k = p.tile_sum[t];
+        p.tile_sum[t] = run;
         run += k;
     }
     if (threadIdx.x == blockDim.x - 1)
         p.cell_start[nc] = run;
+}
+
+// Pass 3: adds each tile's offset, primes the fill cursors and clears the counts for the next
+// rebuild.
+__global__ void __launch_bounds__(1024) k_scan_add(Params p)
+{
+    Ctl *ctl = p.ctl;
+    if (status_of(ctl) & kRebuildBlocking)
+        return;
+    const int nc = ctl->gnx * ctl->gny * ctl->gnz;
+    const int base = blockIdx.x * kScanTile;
+    if (base >= nc)
+        return;
+    const int off = p.tile_sum[blockIdx.x];
+    const int c0 = base + 4 * threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        const int c = c0 + k;
+        if (c < nc)
+        {
+            const int st = p.cell_start[c] + off;
+            p.cell_start[c] = st;
+            p.cell_fill[c] = st;
+            p.cell_cnt[c] = 0;
+        }
+    }
 }
 
 __global__ void __launch_bounds__(kBuildBlock) k_cell_place(Params p)
@@ -765,17 +849,20 @@ int launch_rebuild(const Params &p, cudaStream_t st)
         launched += launch_batch_grid(p, st);
     else
     {
+        const int tiles = p.cell_cap / kScanTile + 1;
         k_bbox<<<bb, kBboxBlock, 0, st>>>(p);
         k_cell_count<<<nb, kBuildBlock, 0, st>>>(p);
-        k_cell_scan<<<1, 1024, 0, st>>>(p);
-        launched += 3;
+        k_scan_tiles<<<tiles, 1024, 0, st>>>(p);
+        k_scan_top<<<1, 1024, 0, st>>>(p);
+        k_scan_add<<<tiles, 1024, 0, st>>>(p);
+        launched += 5;
     }
     k_cell_place<<<nb, kBuildBlock, 0, st>>>(p);
     k_cell_sort<<<1216, kBuildBlock, 0, st>>>(p);
     k_reorder<<<nb, kBuildBlock, 0, st>>>(p);
     k_spring_ell<<<nbp, kBuildBlock, 0, st>>>(p);
     launched += 4;
-    if (p.nsys > 0)
+    if (p.nsys > 0 || p.pl_sparse)
         return launched + launch_batch_pairlist(p, st);
     // one block per cell of the grid (its size is only known on the device: cover the capacity;
     // blocks past the last cell return at once)

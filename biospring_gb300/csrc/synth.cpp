@@ -53,6 +53,13 @@ struct Buckets
         next[id] = head[c];
         head[c] = id;
     }
+    // Removes `id`, which must be the latest insertion into its bucket.
+    void pop(int64_t id, const double * p)
+    {
+        const int64_t c = (coord(p[2]) * dim + coord(p[1])) * dim + coord(p[0]);
+        if (head[c] == id)
+            head[c] = next[id];
+    }
     // True if some stored point other than `skip` lies closer than r to p.
     bool any_within(const double * p, double r, const std::vector<double> & pts, int64_t skip) const
     {
@@ -84,8 +91,9 @@ extern "C" {
 
 // Confined self-avoiding walk of n beads with fixed bond length `step`, kept
 // inside a ball whose uniform-filling radius of gyration is rg_target
-// (R = sqrt(5/3) * rg_target); non-bonded beads stay >= min_sep apart. When a
-// bead cannot be placed after many trials the ball grows by 1%. Writes float
+// (R = sqrt(5/3) * rg_target); non-bonded beads stay >= min_sep apart. When a bead
+// cannot be placed in 200 trials the walk steps back 1 to 8 beads; after 4n such
+// backtracks the ball grows by 1%. Writes float
 // xyz[3n] centred on the origin and returns the radius actually used.
 double bs_synth_ca_chain(int64_t n, uint64_t seed, double step, double rg_target, double min_sep, float * xyz)
 {
@@ -97,23 +105,13 @@ double bs_synth_ca_chain(int64_t n, uint64_t seed, double step, double rg_target
     if (n <= 0)
         return R;
     grid.insert(0, &pts[0]);
-    for (int64_t i = 1; i < n; ++i)
+    int64_t i = 1;
+    long long backtracks = 0;
+    while (i < n)
     {
         bool placed = false;
-        for (int attempt = 0; !placed; ++attempt)
+        for (int attempt = 0; attempt < 200 && !placed; ++attempt)
         {
-            if (attempt >= 50000)
-            {
-                // the chain end is walled in by its own beads: start the walk again in a
-                // slightly larger ball (same random stream)
-                std::fill(grid.head.begin(), grid.head.end(), -1);
-                grid.insert(0, &pts[0]);
-                R *= 1.02;
-                i = 1;
-                attempt = 0;
-            }
-            if (attempt > 0 && attempt % 200 == 0)
-                R *= 1.01;
             double d[3], len2;
             do
             {
@@ -134,6 +132,22 @@ double bs_synth_ca_chain(int64_t n, uint64_t seed, double step, double rg_target
             grid.insert(i, c);
             placed = true;
         }
+        if (placed)
+        {
+            ++i;
+            continue;
+        }
+        // The chain end is walled in: step back 1 to 8 beads (the most recent insertions, so
+        // each is at the head of its bucket) and grow again. The ball grows by 1% only if
+        // backtracking keeps failing.
+        const int64_t back = std::min<int64_t>(i - 1, 1 + static_cast<int64_t>(rng.next() % 8));
+        for (int64_t k = 0; k < back; ++k)
+        {
+            --i;
+            grid.pop(i, &pts[3 * i]);
+        }
+        if (++backtracks % (4 * n) == 0)
+            R *= 1.01;
     }
     double cx = 0, cy = 0, cz = 0;
     for (int64_t i = 0; i < n; ++i)

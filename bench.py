@@ -11,6 +11,15 @@ untimed); each step (the rebuild every 10th step, then the step kernel) is brack
 events on the library's stream. ``e2e`` drives the same steps through the C ABI with host
 buffers: per step, external forces H2D from pinned memory, one bs_step call, energies D2H.
 
+Two more figures ride on the same line (rank 0, one GPU):
+  batched  512 independent Calpha networks (sizes log-uniform in 200..20,000, ~2.1M particles),
+           springs < 10 A, linear steric 8 A, viscosity, rebuild every 10 steps, stepped by the
+           persistent clustered kernel with the autotuned shape, against the same systems stepped
+           one after another through the single-system path (inputs larger than L2);
+  adjoint  loss and dL/dk, dL/dr0 of all springs of a 10,000-particle network after 200 steps with
+           checkpoints every 20 (precise positions), timed against the plain 200-step forward of
+           the same system (L2 flushed before every timed call).
+
 Reference arm (--impl reference): the CPU restatement of the reference's step (the reference
 itself cannot be built where the sources are absent) timed on all host cores with OpenMP.
 
@@ -33,7 +42,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "particle-steps/s (100k-particle plain step)"
+METRIC = "particle-steps/s (100k-particle plain step; batched and adjoint/forward beside it)"
 UNIT = "particle-steps/s"
 N_PARTICLES = 100_000
 BOX = 160.0
@@ -264,12 +273,142 @@ def run_native(args) -> dict:
         "clocks": clocks,
         "interactions": {k: alg[k] for k in ("unique_lj_pairs", "unique_coulomb_pairs")},
     }
+    net.close()
+    if rank == 0 and world == 1 and not args.no_extras:
+        out["batched"] = run_batched()
+        out["adjoint"] = run_adjoint()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(system, seconds=args.cpu_seconds)
-    net.close()
     if dist is not None:
         dist.destroy_process_group()
     return out if rank == 0 else None
+
+
+def run_batched(steps: int = 100) -> dict:
+    """The batched ensemble against its systems stepped one after another."""
+    import torch
+    from biospring_gb300 import SpringNetwork, workloads as W
+
+    ens = W.ensemble(W.ensemble_sizes(), seed=2024)
+    off = ens.meta["offsets"]
+    nsys = len(off) - 1
+    net = SpringNetwork()
+    net.addParticles(xyz=ens.xyz)
+    net.addSprings(ens.ij, ens.r0, ens.k)
+    net.setSystems(off)
+    net.setup(ens.bs_config())
+    net.computeStep(3 * REBUILD)
+    shape = net.batchAutotune()
+    net.computeStep(3 * REBUILD)
+    stream = torch.cuda.ExternalStream(net.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    launches0 = net.launchCount()
+    net.synchronize()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    net.computeStepAsync(steps)
+    e1.record(stream)
+    net.synchronize()
+    torch.cuda.synchronize()
+    launches = net.launchCount() - launches0
+    ms = e0.elapsed_time(e1)
+    batched = ens.n * steps / (ms * 1e-3)
+    net.close()
+    # the same systems, one handle each, stepped one after another (2 periods each)
+    seq_steps = 2 * REBUILD
+    nets = []
+    for b in range(nsys):
+        i0, i1 = int(off[b]), int(off[b + 1])
+        m = (ens.ij[:, 0] >= i0) & (ens.ij[:, 0] < i1)
+        h = SpringNetwork()
+        h.addParticles(xyz=ens.xyz[i0:i1])
+        h.addSprings(ens.ij[m] - i0, ens.r0[m], ens.k[m])
+        h.setup(ens.bs_config())
+        h.computeStep(REBUILD)
+        nets.append(h)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for h in nets:
+        h.computeStep(seq_steps)
+    torch.cuda.synchronize()
+    seq_s = time.perf_counter() - t0
+    for h in nets:
+        h.close()
+    sequential = ens.n * seq_steps / seq_s
+    dbar = 2.0 * ens.ij.shape[0] / ens.n
+    step_bytes = STEP_BYTES_PER_PARTICLE_BASE + SPRING_BYTES_PER_ENTRY * dbar
+    pk = peaks()
+    return {
+        "value": batched, "unit": UNIT, "systems": nsys, "particles": int(ens.n),
+        "steps": steps, "ms_per_step": ms / steps, "gpu_launches": int(launches),
+        "shape": {"block": shape[0], "lanes": shape[1], "cluster": shape[2], "picked_by": "bs_batch_autotune"},
+        "sequential_plain": {"value": sequential, "unit": UNIT,
+                             "how": f"each system alone through bs_step({seq_steps}), one after another"},
+        "speedup_vs_sequential": batched / sequential,
+        "roofline": {"bound": "hbm", "achieved": batched * step_bytes / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": batched * step_bytes / 1e9 / pk["hbm_gbs"], "peak_src": pk["src"],
+                     "bytes_per_particle_step": step_bytes},
+        "workload": "512 Calpha networks, sizes log-uniform 200..20000 (seed 2024), springs < 10 A "
+                    f"(mean degree {dbar:.1f}), linear steric 8 A, viscosity 1, dt 0.01 fs, rebuild every 10",
+        "l2": "inputs larger than L2",
+    }
+
+
+def run_adjoint(reps: int = 5) -> dict:
+    """Adjoint (loss + gradients) against the plain forward of the same 200 steps."""
+    import torch
+    from biospring_gb300 import SpringNetwork, workloads as W
+
+    s, target, nsteps = W.adjoint_fit(10_000, seed=4)
+    s.config["precise_positions"] = 1
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def handle():
+        h = SpringNetwork()
+        h.addParticles(**{k: v for k, v in s.arrays().items() if v is not None})
+        h.addSprings(s.ij, s.r0, s.k)
+        h.setup(s.bs_config())
+        return h
+
+    fwd, adj = handle(), handle()
+    x0 = fwd.getPositions()
+    fwd.computeStep(nsteps)
+    adj.adjoint(nsteps, target, 20)
+
+    def timed(fn, before=None):
+        ts = []
+        for _ in range(reps):
+            if before:
+                before()
+            flush.zero_()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t)
+        return statistics.median(ts)
+
+    t_fwd = timed(lambda: fwd.computeStep(nsteps), before=lambda: fwd.setPositions(x0))
+    result = {}
+
+    def run_adj():
+        result["r"] = adj.adjoint(nsteps, target, 20)
+
+    t_adj = timed(run_adj)
+    launches0 = adj.launchCount()
+    run_adj()
+    launches = adj.launchCount() - launches0
+    loss, gk, gr = result["r"]
+    fwd.close()
+    adj.close()
+    return {
+        "ratio": t_adj / t_fwd, "adjoint_ms": t_adj * 1e3, "forward_ms": t_fwd * 1e3, "loss": loss,
+        "gradients": int(2 * gk.shape[0]), "gpu_launches": int(launches),
+        "workload": f"Calpha network N={s.n} ({s.ij.shape[0]} springs), target = start + smooth 2 A field, "
+                    f"{nsteps} steps, checkpoints every 20, precise positions",
+        "timing": "median wall time of bs_adjoint vs bs_step(200) from the same state, L2 flushed before each",
+    }
 
 
 def cpu_baseline(system, seconds: float = 15.0) -> dict:
@@ -323,6 +462,7 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and adjoint figures")
     args = ap.parse_args()
     if args.impl == "reference":
         if args.steps > 20:

@@ -174,8 +174,12 @@ void release_device(bs_sim *s)
     s->ready = false;
 }
 
-float band_lo2(double c) { return static_cast<float>((c * (1.0 - 1.0 / 16384.0)) * (c * (1.0 - 1.0 / 16384.0))); }
-float band_hi2(double c) { return static_cast<float>((c * (1.0 + 1.0 / 16384.0)) * (c * (1.0 + 1.0 / 16384.0))); }
+// Guard band on r^2 around a cutoff c: c (1 -+ 2^-19), squared. The FP32 squared distance of a
+// pair is within ~6 * 2^-24 (relative) of the exact one and the reference's float-rounded distance
+// within 2^-23 on the square, so outside the band (+-2^-18 on r^2, about ten times wider) the FP32
+// value classifies the pair exactly; inside it the FP64 reference test decides.
+float band_lo2(double c) { return static_cast<float>((c * (1.0 - 1.0 / 524288.0)) * (c * (1.0 - 1.0 / 524288.0))); }
+float band_hi2(double c) { return static_cast<float>((c * (1.0 + 1.0 / 524288.0)) * (c * (1.0 + 1.0 / 524288.0))); }
 
 // Reads the control block back (synchronises the handle's stream).
 int read_ctl(bs_sim *s)
@@ -616,8 +620,8 @@ int bs_set_rigid_bodies(bs_sim *s, int32_t nb, const int32_t *offsets, const int
     std::vector<uint8_t> seen(s->n, 0);
     for (int32_t b = 0; b < nb; ++b)
     {
-        if (offsets[b + 1] < offsets[b])
-            return fail(s, BS_E_ARG, "bs_set_rigid_bodies: offsets must be non-decreasing");
+        if (offsets[b + 1] <= offsets[b])
+            return fail(s, BS_E_ARG, "bs_set_rigid_bodies: every body needs at least one particle");
         for (int32_t t = offsets[b]; t < offsets[b + 1]; ++t)
         {
             const int32_t id = ids[t];
@@ -625,13 +629,15 @@ int bs_set_rigid_bodies(bs_sim *s, int32_t nb, const int32_t *offsets, const int
                 return fail(s, BS_E_ARG, "bs_set_rigid_bodies: particle id out of range");
             if (seen[id])
                 return fail(s, BS_E_ARG, "bs_set_rigid_bodies: a particle belongs to two bodies");
+            if (s->is_static[id])
+                return fail(s, BS_E_ARG, "bs_set_rigid_bodies: a static particle cannot belong to a rigid body");
             seen[id] = 1;
             bodies[b].push_back(id);
         }
     }
     s->bodies = bodies;
     s->ready = false;
-    return fail(s, BS_E_STATE, "bs_set_rigid_bodies: rigid-body dynamics are not available in this build");
+    return BS_OK;
 }
 
 int bs_setup(bs_sim *s, const bs_config *cfg)
@@ -657,8 +663,6 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
         return fail(s, BS_E_ARG, "cuda.rebuildevery must be >= 1");
     if (!(c.list_skin >= 0.0))
         return fail(s, BS_E_ARG, "cuda.listskin must be >= 0");
-    if (c.rigidbody_enable && !s->bodies.empty())
-        return fail(s, BS_E_STATE, "rigid-body dynamics are not available in this build");
     if (s->n == 0)
         return fail(s, BS_E_ARG, "bs_setup: no particles");
     const bool batch = !s->sys_off.empty();
@@ -691,6 +695,15 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     p.n = static_cast<int>(n);
     p.npad = static_cast<int>((n + 31) / 32 * 32);
     const int npad = p.npad;
+
+    // ---- rigid bodies (RigidBodiesManager::InitRigidBodies, RigidBodiesManager.cpp:11-43):
+    // members are rigid only when rigidbody.enable is set ----
+    const bool bodies_on = c.rigidbody_enable && !s->bodies.empty();
+    s->rigid.assign(n, 0);
+    if (bodies_on)
+        for (const auto &body : s->bodies)
+            for (int32_t id : body)
+                s->rigid[id] = 1;
 
     // ---- spring CSR in caller order (both directions) ----
     std::vector<int> deg(n, 0);
@@ -849,6 +862,8 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
         if (on[t])
             list_radius = std::max(list_radius, R);
     }
+    if (!(on[0] || on[1] || on[2] || on[3]))
+        list_radius = 1.0e4; // no nonbonded term: a grid of a few cells keeps the rebuild trivial
     p.list_radius = static_cast<float>(list_radius);
     // grid cells and density from the bounding box of each system (one system unless batched)
     const int nsys = batch ? static_cast<int>(s->sys_off.size() - 1) : 1;
@@ -946,6 +961,66 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
         s->ctl_host->bbox_enc[3 + k] = 0u;
     }
     BS_CUDA(cudaMemcpyAsync(p.ctl, s->ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, s->stream));
+
+    // ---- rigid-body state (RigidBody.cpp:57-123): total mass (FP64 sum), mass-weighted
+    // barycentre and member offsets in float, sphere inertia 2/5 M (radius 1) ----
+    if (bodies_on)
+    {
+        const int nb = static_cast<int>(s->bodies.size());
+        std::vector<BodyState> bs(nb);
+        std::vector<int> start(nb + 1, 0), ids;
+        std::vector<float4> p0;
+        for (int b = 0; b < nb; ++b)
+        {
+            const auto &mem = s->bodies[b];
+            double m = 0.0;
+            for (int32_t i : mem)
+                m += s->mass[i];
+            float bx = 0.f, by = 0.f, bz = 0.f;
+            double tm = 0.0;
+            for (int32_t i : mem)
+            {
+                bx = bx + s->xyz[3 * i] * s->mass[i];
+                by = by + s->xyz[3 * i + 1] * s->mass[i];
+                bz = bz + s->xyz[3 * i + 2] * s->mass[i];
+                tm = tm + s->mass[i];
+            }
+            const float inv_tm = static_cast<float>(1.0 / tm);
+            bx = bx * inv_tm;
+            by = by * inv_tm;
+            bz = bz * inv_tm;
+            BodyState st{};
+            st.pos = make_float4(bx, by, bz, 0.f);
+            st.vel = make_float4(0.f, 0.f, 0.f, 0.f);
+            st.L = make_float4(0.f, 0.f, 0.f, 0.f);
+            st.q = make_float4(0.f, 0.f, 0.f, 1.f);
+            st.mass = m;
+            st.ibodyinv = 1.0 / ((2.0 / 5.0) * m * 1.0 * 1.0);
+            bs[b] = st;
+            for (int32_t i : mem)
+            {
+                ids.push_back(i);
+                p0.push_back(make_float4(s->xyz[3 * i] - bx, s->xyz[3 * i + 1] - by, s->xyz[3 * i + 2] - bz, 0.f));
+            }
+            start[b + 1] = static_cast<int>(ids.size());
+        }
+        int *d_start, *d_ids;
+        float4 *d_p0;
+        BS_CUDA(s->dev.alloc(&p.body, nb));
+        BS_CUDA(s->dev.alloc(&d_start, nb + 1));
+        BS_CUDA(s->dev.alloc(&d_ids, ids.size()));
+        BS_CUDA(s->dev.alloc(&d_p0, p0.size()));
+        BS_CUDA(s->dev.alloc(&p.rforce, npad));
+        BS_CUDA(cudaMemcpyAsync(p.body, bs.data(), sizeof(BodyState) * nb, cudaMemcpyHostToDevice, s->stream));
+        BS_CUDA(cudaMemcpyAsync(d_start, start.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, s->stream));
+        BS_CUDA(cudaMemcpyAsync(d_ids, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice, s->stream));
+        BS_CUDA(cudaMemcpyAsync(d_p0, p0.data(), sizeof(float4) * p0.size(), cudaMemcpyHostToDevice, s->stream));
+        BS_CUDA(cudaMemsetAsync(p.rforce, 0, sizeof(float4) * npad, s->stream));
+        p.body_start = d_start;
+        p.body_ids = d_ids;
+        p.body_p0 = d_p0;
+        p.nbody = nb;
+    }
 
     // ---- step parameters ----
     p.dt = static_cast<float>(c.timestep);
@@ -1762,6 +1837,8 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
                                  "disable coulomb, hydrophobicity and impala");
     if (c.steric_enable && c.steric_mode != BS_STERIC_LINEAR)
         return fail(s, BS_E_ARG, "bs_adjoint: only the linear steric mode is differentiated");
+    if (s->p.nbody > 0)
+        return fail(s, BS_E_ARG, "bs_adjoint: rigid bodies are not differentiated");
     if (s->ext_dirty)
         return fail(s, BS_E_STATE, "bs_adjoint: an external force is pending; step or clear it first");
     int rc = bs_synchronize(s);

@@ -87,6 +87,20 @@ struct Ctl
     int lagging;               // live systems behind `nominal` (stopped early by a stale list)
     int dead;                  // systems with a non-finite position
     int stale_events;          // rebuilds that found a stale list (counted, never reset)
+    long long rigid_steps;     // value of `steps` for which the rigid bodies last moved
+    unsigned int done_rigid;   // last-block counter of the body kernel
+};
+
+// State of one rigid body (RigidBody.h): position, velocity, angular momentum, orientation
+// (x, y, z, w), total mass and the inverse of its diagonal inertia.
+struct BodyState
+{
+    float4 pos;
+    float4 vel;
+    float4 L;
+    float4 q;
+    double mass;
+    double ibodyinv;
 };
 
 // Search grid of one system of a batched ensemble (same formula as the single-system grid).
@@ -193,6 +207,13 @@ struct Params
     const int *cl_start;      // [ncl + 1] systems of each cluster of the persistent kernel
     const int *cl_sys;        // [nsys]
     int ncl;
+    // rigid bodies (nbody = 0: none)
+    int nbody;
+    BodyState *body;          // [nbody]
+    const int *body_start;    // [nbody + 1] member ranges
+    const int *body_ids;      // caller ids of the members, in the caller's order per body
+    const float4 *body_p0;    // member position relative to the barycentre at set-up
+    float4 *rforce;           // [npad] total force on each rigid particle in the current step
 };
 
 constexpr int kMaxCluster = 16;

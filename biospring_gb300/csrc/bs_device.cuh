@@ -551,6 +551,12 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             {
                 p.force_out[p.perm[lb][s]] = make_float4(fx, fy, fz, 0.f);
             }
+            else if (fi & PF_RIGID)
+            {
+                // a rigid particle's force goes to its body (RigidBody.cpp:567-580); the body
+                // kernel moves the particle, and its kinetic energy counts as zero
+                p.rforce[s] = make_float4(fx, fy, fz, 0.f);
+            }
             else
             {
                 // ---- semi-implicit Euler (Particle.cpp:109-128), no fused multiply-adds ----

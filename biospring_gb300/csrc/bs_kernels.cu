@@ -898,6 +898,14 @@ static void launch_step_lanes(const Params &p, cudaStream_t st)
 
 int launch_step(const Params &p, int mode, cudaStream_t st)
 {
+    int launched = launch_step_only(p, mode, st);
+    if (mode == MODE_STEP && p.nbody > 0)
+        launched += launch_rigid(p, st); // after the step kernel, on the same stream
+    return launched;
+}
+
+int launch_step_only(const Params &p, int mode, cudaStream_t st)
+{
 #define BS_STEP_CASE(SMV)                                                                                              \
     case SMV:                                                                                                          \
         if (mode == MODE_STEP)                                                                                         \

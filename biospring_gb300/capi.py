@@ -74,6 +74,16 @@ class BsConfig(C.Structure):
         ("rebuild_every", C.c_int32),
         ("list_skin", C.c_double),
         ("precise_positions", C.c_int32),
+        ("probe_enable", C.c_int32),
+        ("probe_electrostatic", C.c_int32),
+        ("probe_steric", C.c_int32),
+        ("probe_x", C.c_double),
+        ("probe_y", C.c_double),
+        ("probe_z", C.c_double),
+        ("probe_mass", C.c_double),
+        ("probe_epsilon", C.c_double),
+        ("probe_radius", C.c_double),
+        ("probe_charge", C.c_double),
     ]
 
     def to_dict(self) -> dict:
@@ -117,6 +127,7 @@ SIGNATURES = {
     "bs_get_launch_count": (C.c_int, [C.c_void_p, _i64p]),
     "bs_last_error": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "bs_set_systems": (C.c_int, [C.c_void_p, C.c_int32, _i64p]),
+    "bs_get_probe": (C.c_int, [C.c_void_p, _f32p]),
     "bs_get_spring_count": (C.c_int, [C.c_void_p, _i64p]),
     "bs_set_spring_parameters": (C.c_int, [C.c_void_p, _f32p, _f32p]),
     "bs_adjoint": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _f32p, _f64p, _f32p, _f32p, _f32p]),

@@ -512,6 +512,11 @@ int bs_default_config(bs_config *c)
     c->impala_alpha = 1.99;
     c->rebuild_every = 10;
     c->list_skin = 1.0;
+    c->probe_x = c->probe_y = c->probe_z = 1.0;
+    c->probe_mass = 1.0;
+    c->probe_epsilon = 1.0;
+    c->probe_radius = 1.0;
+    c->probe_charge = 0.0;
     return BS_OK;
 }
 
@@ -673,6 +678,8 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
             return fail(s, BS_E_ARG, "bs_set_systems: the offsets must end at the particle count");
         if (!s->bodies.empty())
             return fail(s, BS_E_ARG, "rigid bodies are not available for batched ensembles");
+        if (c.probe_enable)
+            return fail(s, BS_E_ARG, "the probe is not available for batched ensembles");
         std::vector<int> sys_of_id(s->n);
         max_sys = 0;
         for (size_t b = 0; b + 1 < s->sys_off.size(); ++b)
@@ -959,6 +966,34 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     {
         s->ctl_host->bbox_enc[k] = 0xffffffffu;
         s->ctl_host->bbox_enc[3 + k] = 0u;
+    }
+    // ---- probe (SpringNetwork::_setupProbe, SpringNetwork.cpp:749-766): steric factors as a
+    // particle's, state in the control block ----
+    if (c.probe_enable)
+    {
+        const double eps = static_cast<float>(c.probe_epsilon), rad = static_cast<float>(c.probe_radius);
+        double P = rad, F = 0.0;
+        if (c.steric_mode == BS_STERIC_LJ_12_6_AMBER || c.steric_mode == BS_STERIC_LJ_8_6_LEWITT)
+        {
+            P = std::sqrt(eps) * rad * rad * rad;
+            F = std::sqrt(eps) * std::pow(rad, c.steric_mode == BS_STERIC_LJ_12_6_AMBER ? 6 : 4);
+        }
+        else if (c.steric_mode == BS_STERIC_LJ_8_6_ZACHARIAS)
+        {
+            P = eps * std::pow(rad, 6);
+            F = eps * std::pow(rad, 8);
+        }
+        p.probe_on = 1;
+        p.probe_steric = c.probe_steric != 0;
+        p.probe_elec = c.probe_electrostatic != 0;
+        p.probe_P = static_cast<float>(P);
+        p.probe_F = static_cast<float>(F);
+        p.probe_q = static_cast<float>(c.probe_charge);
+        p.probe_mass = static_cast<float>(c.probe_mass);
+        BS_CUDA(s->dev.alloc(&p.probe_f, npad));
+        BS_CUDA(cudaMemsetAsync(p.probe_f, 0, sizeof(float4) * npad, s->stream));
+        s->ctl_host->probe_pos = make_float4(static_cast<float>(c.probe_x), static_cast<float>(c.probe_y),
+                                             static_cast<float>(c.probe_z), 0.f);
     }
     BS_CUDA(cudaMemcpyAsync(p.ctl, s->ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, s->stream));
 
@@ -1705,6 +1740,24 @@ int bs_get_system_energies(bs_sim *s, double *out)
     return BS_OK;
 }
 
+int bs_get_probe(bs_sim *s, float state[6])
+{
+    if (!s || !state)
+        return fail(s, BS_E_ARG, "bs_get_probe: null argument");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "call bs_setup first");
+    int rc = bs_synchronize(s);
+    if (rc == BS_OK)
+        rc = read_ctl(s);
+    if (rc)
+        return rc;
+    const Ctl &h = *s->ctl_host;
+    const float v[6] = {h.probe_pos.x, h.probe_pos.y, h.probe_pos.z, h.probe_vel.x, h.probe_vel.y, h.probe_vel.z};
+    for (int k = 0; k < 6; ++k)
+        state[k] = s->p.probe_on ? v[k] : 0.0f;
+    return BS_OK;
+}
+
 int bs_get_spring_count(bs_sim *s, int64_t *count)
 {
     if (!s || !count)
@@ -1837,8 +1890,8 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
                                  "disable coulomb, hydrophobicity and impala");
     if (c.steric_enable && c.steric_mode != BS_STERIC_LINEAR)
         return fail(s, BS_E_ARG, "bs_adjoint: only the linear steric mode is differentiated");
-    if (s->p.nbody > 0)
-        return fail(s, BS_E_ARG, "bs_adjoint: rigid bodies are not differentiated");
+    if (s->p.nbody > 0 || s->p.probe_on)
+        return fail(s, BS_E_ARG, "bs_adjoint: rigid bodies and the probe are not differentiated");
     if (s->ext_dirty)
         return fail(s, BS_E_STATE, "bs_adjoint: an external force is pending; step or clear it first");
     int rc = bs_synchronize(s);

@@ -89,6 +89,10 @@ struct Ctl
     int stale_events;          // rebuilds that found a stale list (counted, never reset)
     long long rigid_steps;     // value of `steps` for which the rigid bodies last moved
     unsigned int done_rigid;   // last-block counter of the body kernel
+    // probe particle (SpringNetwork.cpp:749-766)
+    float4 probe_pos;
+    float4 probe_vel;
+    long long probe_steps;     // value of `steps` for which the probe last moved
 };
 
 // State of one rigid body (RigidBody.h): position, velocity, angular momentum, orientation
@@ -214,6 +218,11 @@ struct Params
     const int *body_ids;      // caller ids of the members, in the caller's order per body
     const float4 *body_p0;    // member position relative to the barycentre at set-up
     float4 *rforce;           // [npad] total force on each rigid particle in the current step
+    // probe (probe_on = 0: none): its steric factors (P, F as the particles'), charge and mass,
+    // and the reaction of every slot on it in the current step
+    int probe_on, probe_steric, probe_elec;
+    float probe_P, probe_F, probe_q, probe_mass;
+    float4 *probe_f;          // [npad]
 };
 
 constexpr int kMaxCluster = 16;

@@ -397,6 +397,78 @@ __device__ __forceinline__ void hydro_forces(const Params &p, int s, int t, floa
     }
 }
 
+// Force of the probe on one dynamic particle at pi and the particle's share of the pair energies
+// (Particle::addStericProbeForce / addElectrostaticProbeForce, Particle.cpp:434-465): no cutoff,
+// the full pair energy counts (the reference adds it to the totals once per particle). The same
+// pair kernels as the list terms, with the probe's own steric factors.
+template <int SM>
+__device__ __forceinline__ void probe_pair(const Params &p, const float4 &prb, float4 pi, float fhi_i, float qi,
+                                           float &fx, float &fy, float &fz, float &es, float &ec)
+{
+    const float dx = prb.x - pi.x, dy = prb.y - pi.y, dz = prb.z - pi.z;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (p.probe_steric)
+    {
+        float fod = 0.0f;
+        if (SM == BS_STERIC_LINEAR)
+        {
+            const float d = sqrtf(r2);
+            const float dv = d - (p.probe_P + pi.w);
+            if (dv <= 0.0f)
+            {
+                es = fmaf(0.5f * p.steric_scale, dv * dv, es);
+                fod = d > 0.0f ? dv / d : 0.0f;
+            }
+        }
+        else if (r2 >= 0.01f)
+        {
+            const float inv2 = recip_nr(r2);
+            const float i6 = inv2 * inv2 * inv2;
+            const float t6 = p.probe_P * pi.w * i6;
+            if (SM == BS_STERIC_LJ_12_6_AMBER)
+            {
+                const float t12 = p.probe_F * fhi_i * i6 * i6;
+                es = fmaf(p.steric_scale, t12 - 2.0f * t6, es);
+                fod = 12.0f * (t6 - t12) * inv2;
+            }
+            else if (SM == BS_STERIC_LJ_8_6_LEWITT)
+            {
+                const float t8 = p.probe_F * fhi_i * i6 * inv2;
+                es = fmaf(p.steric_scale, 3.0f * t8 - 4.0f * t6, es);
+                fod = 24.0f * (t6 - t8) * inv2;
+            }
+            else
+            {
+                const float t8 = p.probe_F * fhi_i * i6 * inv2;
+                es = fmaf(p.steric_scale, t8 - t6, es);
+                fod = (6.0f * t6 - 8.0f * t8) * inv2;
+            }
+        }
+        const float k = fod * p.k_spring_f * p.steric_scale;
+        fx = fmaf(dx, k, fx);
+        fy = fmaf(dy, k, fy);
+        fz = fmaf(dz, k, fz);
+    }
+    if (p.probe_elec && r2 >= 1e-6f) // d < 0.001 A gives zero (electrostatic.hpp:18-19)
+    {
+        const float inv = rsqrt_nr(r2);
+        float tq = p.probe_q * qi * inv;
+        float fod;
+        if (p.dielectric_mode == BS_DIELECTRIC_DISTANCE)
+        {
+            tq *= inv;
+            fod = -2.0f * tq * inv * inv;
+        }
+        else
+            fod = -tq * inv * inv;
+        ec = fmaf(tq, p.k_elec_e, ec);
+        const float k = fod * p.k_elec_f;
+        fx = fmaf(dx, k, fx);
+        fy = fmaf(dy, k, fy);
+        fz = fmaf(dz, k, fz);
+    }
+}
+
 // Sum over the T consecutive lanes of a particle group (result in every lane of the group).
 template <int T> __device__ __forceinline__ float group_sum(float v)
 {
@@ -509,6 +581,8 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             }
             else
                 p.force_out[p.perm[lb][s]] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (p.probe_on)
+                p.probe_f[s] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         else
         {
@@ -546,6 +620,17 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
                 fz += xf.z;
                 if (MODE == MODE_STEP && (xf.x != 0.f || xf.y != 0.f || xf.z != 0.f))
                     p.ext[id] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            // ---- probe (SpringNetwork.cpp:156-182), after every other term ----
+            if (p.probe_on)
+            {
+                const float4 prb = p.ctl->probe_pos;
+                float px = 0.f, py = 0.f, pz = 0.f;
+                probe_pair<SM>(p, prb, pi, p.fhi[lb][s], p.chg[lb][s], px, py, pz, e[1], e[2]);
+                fx += px;
+                fy += py;
+                fz += pz;
+                p.probe_f[s] = make_float4(-px, -py, -pz, 0.f);
             }
             if (MODE == MODE_FORCES)
             {

@@ -647,6 +647,79 @@ __global__ void __launch_bounds__(kStepBlock, kStepMinBlocks) k_step(Params p)
     }
 }
 
+// The probe's own step, after the step kernel (SpringNetwork.cpp:156-182): the sum of the
+// particles' reactions (float-float, fixed order), viscosity from its velocity, the Euler step
+// (Particle.cpp:109-128) and its kinetic energy, added to the step's total. One block.
+__global__ void __launch_bounds__(1024) k_probe(Params p)
+{
+    Ctl *ctl = p.ctl;
+    const long long steps = *(volatile const long long *)&ctl->steps;
+    if (steps == ctl->probe_steps)
+        return; // the step kernel did not run
+    float acc[3][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (int s = threadIdx.x; s < p.n; s += blockDim.x)
+    {
+        const float4 f = p.probe_f[s];
+        ff_add(acc[0][0], acc[0][1], f.x, 0.f);
+        ff_add(acc[1][0], acc[1][1], f.y, 0.f);
+        ff_add(acc[2][0], acc[2][1], f.z, 0.f);
+    }
+    __shared__ float sh[3][2][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        float hi = acc[k][0], lo = acc[k][1];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
+            const float l2 = __shfl_down_sync(0xffffffffu, lo, o);
+            ff_add(hi, lo, h2, l2);
+        }
+        if (lane == 0)
+        {
+            sh[k][0][warp] = hi;
+            sh[k][1][warp] = lo;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x != 0)
+        return;
+    float F[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        float hi = 0.f, lo = 0.f;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w)
+            ff_add(hi, lo, sh[k][0][w], sh[k][1][w]);
+        F[k] = __fadd_rn(hi, lo);
+    }
+    float4 v = ctl->probe_vel, x = ctl->probe_pos;
+    if (p.visc_on)
+    {
+        F[0] = __fsub_rn(F[0], __fmul_rn(v.x, p.visc));
+        F[1] = __fsub_rn(F[1], __fmul_rn(v.y, p.visc));
+        F[2] = __fsub_rn(F[2], __fmul_rn(v.z, p.visc));
+    }
+    const float m = p.probe_mass;
+    if (m > 0.0f)
+    {
+        v.x = __fadd_rn(v.x, __fmul_rn(__fdiv_rn(F[0], m), p.dt));
+        v.y = __fadd_rn(v.y, __fmul_rn(__fdiv_rn(F[1], m), p.dt));
+        v.z = __fadd_rn(v.z, __fmul_rn(__fdiv_rn(F[2], m), p.dt));
+    }
+    const double vx = v.x, vy = v.y, vz = v.z;
+    const float vit = static_cast<float>(sqrt(__dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz))));
+    const float ke = 0.5f * m * (vit * vit) * p.k_kin;
+    x.x = __fadd_rn(x.x, __fmul_rn(v.x, p.dt));
+    x.y = __fadd_rn(x.y, __fmul_rn(v.y, p.dt));
+    x.z = __fadd_rn(x.z, __fmul_rn(v.z, p.dt));
+    ctl->probe_pos = x;
+    ctl->probe_vel = v;
+    ctl->energies[BS_ENERGY_KINETIC] += static_cast<double>(ke);
+    ctl->probe_steps = steps;
+}
+
 // ------------------------------------------------------------------------------------------
 // Host-facing helpers
 // ------------------------------------------------------------------------------------------
@@ -901,6 +974,11 @@ int launch_step(const Params &p, int mode, cudaStream_t st)
     int launched = launch_step_only(p, mode, st);
     if (mode == MODE_STEP && p.nbody > 0)
         launched += launch_rigid(p, st); // after the step kernel, on the same stream
+    if (mode == MODE_STEP && p.probe_on)
+    {
+        k_probe<<<1, 1024, 0, st>>>(p);
+        launched += 1;
+    }
     return launched;
 }
 

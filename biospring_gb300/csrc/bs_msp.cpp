@@ -5,8 +5,8 @@
 // lines starting with '#' and blank lines ignored, unknown and duplicated parameters rejected,
 // booleans spelled true/false/1/0/on/off/yes/no (src/utils/string.hpp:150-161). Every group
 // and parameter name of the reference is accepted (src/configuration/Setting.hpp); the ones
-// the step does not read (trajectories, grids, probe, insertion vector, sampling) are checked
-// for syntax and otherwise ignored. A new group "cuda.*" carries the device-path knobs.
+// the step does not read (trajectories, grids, insertion vector, sampling) are checked for
+// syntax and otherwise ignored. A new group "cuda.*" carries the device-path knobs.
 
 #include <cctype>
 #include <cstdio>
@@ -164,6 +164,12 @@ extern "C" int bs_config_parse_msp(const char *text, bs_config *cfg, char *err, 
                 c.rigidbody_enable = b;
             else if (name == "cuda.precisepositions")
                 c.precise_positions = b;
+            else if (name == "probe.enable")
+                c.probe_enable = b;
+            else if (name == "probe.enableelectrostatic")
+                c.probe_electrostatic = b;
+            else if (name == "probe.enablesteric")
+                c.probe_steric = b;
         }
         else if (name == "steric.mode")
         {
@@ -235,6 +241,20 @@ extern "C" int bs_config_parse_msp(const char *text, bs_config *cfg, char *err, 
                 c.impala_z0 = d;
             else if (name == "cuda.impalaalpha")
                 c.impala_alpha = d;
+            else if (name == "probe.x")
+                c.probe_x = d;
+            else if (name == "probe.y")
+                c.probe_y = d;
+            else if (name == "probe.z")
+                c.probe_z = d;
+            else if (name == "probe.mass")
+                c.probe_mass = d;
+            else if (name == "probe.epsilon")
+                c.probe_epsilon = d;
+            else if (name == "probe.radius")
+                c.probe_radius = d;
+            else if (name == "probe.charge")
+                c.probe_charge = d;
         }
     }
     *cfg = c;

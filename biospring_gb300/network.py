@@ -242,6 +242,12 @@ class SpringNetwork:
         self._check(self._lib.bs_get_cells(self._h, term, ptr(out, C.c_int64)), self._h)
         return out
 
+    def getProbe(self) -> np.ndarray:
+        """Probe position and velocity, float32[6] (SpringNetwork::getProbeParticle)."""
+        out = np.zeros(6, dtype=np.float32)
+        self._check(self._lib.bs_get_probe(self._h, ptr(out, C.c_float)), self._h)
+        return out
+
     def launchCount(self) -> int:
         c = C.c_int64()
         self._check(self._lib.bs_get_launch_count(self._h, C.byref(c)), self._h)

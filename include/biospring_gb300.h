@@ -105,6 +105,13 @@ typedef struct bs_config {
     double list_skin;         /* A; extra radius of the device pair list; drift > skin/2 forces a rebuild */
     int32_t precise_positions; /* carry each position's rounding remainder (float-float x += v dt);
                                   off (0) reproduces the reference's FP32 update */
+    /* probe.* (Configuration.hpp:186-195): one extra interactive particle that every dynamic
+       particle feels without cutoff (SpringNetwork.cpp:156-182) */
+    int32_t probe_enable;
+    int32_t probe_electrostatic; /* probe.enableelectrostatic */
+    int32_t probe_steric;        /* probe.enablesteric */
+    double probe_x, probe_y, probe_z;
+    double probe_mass, probe_epsilon, probe_radius, probe_charge;
 } bs_config;
 
 typedef struct bs_sim bs_sim;
@@ -202,6 +209,12 @@ int bs_set_force(bs_sim *sim, int64_t i, const float f[3]);
 /* Sets the external force of every particle for the next step (float[3n], caller order);
  * the bulk form of bs_set_force used by interactive drivers every step. */
 int bs_set_external_forces(bs_sim *sim, const float *f);
+
+/* Probe position and velocity (float[6]: x, y, z, vx, vy, vz) after the last step; zeros when
+ * probe.enable is off (replaces SpringNetwork::getProbeParticle, SpringNetwork.h:277). The probe
+ * moves with bs_step; a force-only evaluation (bs_compute_forces) applies its force to the
+ * particles but does not move it. */
+int bs_get_probe(bs_sim *sim, float state[6]);
 
 /* Energies of the last step or force evaluation, BS_ENERGY_* order, in kJ/mol
  * (SpringNetwork::getKineticEnergy ... getHydrophobicEnergy, SpringNetwork.h:157-162).

@@ -488,6 +488,13 @@ struct Sim
     std::vector<std::unordered_set<int64_t>> bonded;
     Grid grid[3];
     float energies[BS_NUM_ENERGIES] = {0, 0, 0, 0, 0, 0};
+    // probe particle (SpringNetwork.cpp:749-766): not in the particle lists or the grids
+    struct Probe
+    {
+        V3 pos{1, 1, 1}, vel{0, 0, 0}, force{0, 0, 0};
+        float mass = 1, radius = 1, eps = 1, charge = 0;
+    } probe;
+    bool probe_on = false;
     std::vector<Body> bodies;
     bool rigid_on = false;
 
@@ -689,6 +696,50 @@ struct Sim
             e_imp += pe_imp[i];
             e_hydro += pe_hydro[i];
         }
+        float probe_ke = 0.0f;
+        if (probe_on)
+        {
+            // SpringNetwork.cpp:156-182 and Particle::addStericProbeForce /
+            // addElectrostaticProbeForce (Particle.cpp:434-465): every dynamic particle against the
+            // probe, no cutoff, full pair energy to the totals; then the probe alone moves.
+            probe.force = {0, 0, 0};
+            for (int64_t i : dynamic)
+            {
+                if (cfg.probe_steric)
+                {
+                    V3 f = sub(probe.pos, pos(i));
+                    const float d = norm3(f);
+                    const float pe = ff.steric_energy(probe.radius, radius[i], probe.eps, eps[i], d);
+                    pe_steric[i] += pe * 0.5f;
+                    f = normalize3(f);
+                    f = mul(f, ff.steric_force(probe.radius, radius[i], probe.eps, eps[i], d));
+                    add_force(i, f);
+                    probe.force = add(probe.force, neg(f));
+                    e_steric += pe;
+                }
+                if (cfg.probe_electrostatic)
+                {
+                    V3 f = sub(probe.pos, pos(i));
+                    const float d = norm3(f);
+                    const float pe = ff.elec_energy(probe.charge, charge[i], d);
+                    pe_elec[i] += pe * 0.5f;
+                    f = normalize3(f);
+                    f = mul(f, ff.elec_force(probe.charge, charge[i], d));
+                    add_force(i, f);
+                    probe.force = add(probe.force, neg(f));
+                    e_elec += pe;
+                }
+            }
+            if (cfg.viscosity_enable)
+                probe.force = sub(probe.force, mul(probe.vel, visc));
+            // Particle::IntegrateEuler (Particle.cpp:109-128)
+            const float dt = static_cast<float>(cfg.timestep);
+            if (probe.mass > 0.0f)
+                probe.vel = add(probe.vel, mul(divs(probe.force, probe.mass), dt));
+            const float vit = norm3(probe.vel);
+            probe_ke = static_cast<float>(0.5f * probe.mass * (vit * vit) * C_KINETIC);
+            probe.pos = add(probe.pos, mul(probe.vel, dt));
+        }
         if (rigid_on)
             for (int64_t i : dynamic)
                 if (rigid[i])
@@ -701,6 +752,7 @@ struct Sim
                     b.force = add(b.force, f);
                     b.torque = add(b.torque, tq);
                 }
+        energies[BS_ENERGY_KINETIC] += probe_ke; // before the particles' kinetic energy
         energies[BS_ENERGY_ELECTROSTATIC] = e_elec;
         energies[BS_ENERGY_STERIC] = e_steric;
         energies[BS_ENERGY_IMP] = e_imp;
@@ -948,8 +1000,25 @@ void * bso_create(const bs_config * cfg, int64_t n, const float * xyz, const flo
     ff.hydroscale = static_cast<float>(cfg->hydrophobicity_scale);
     ff.imp_z0 = static_cast<float>(cfg->impala_z0);
     ff.imp_alpha = static_cast<float>(cfg->impala_alpha);
+    // SpringNetwork::_setupProbe (SpringNetwork.cpp:749-766)
+    s->probe_on = cfg->probe_enable != 0;
+    s->probe.pos = {static_cast<float>(cfg->probe_x), static_cast<float>(cfg->probe_y), static_cast<float>(cfg->probe_z)};
+    s->probe.vel = {0, 0, 0};
+    s->probe.mass = static_cast<float>(cfg->probe_mass);
+    s->probe.radius = static_cast<float>(cfg->probe_radius);
+    s->probe.eps = static_cast<float>(cfg->probe_epsilon);
+    s->probe.charge = static_cast<float>(cfg->probe_charge);
     s->setup_grids();
     return s;
+}
+
+// Probe position and velocity (float[6]); zeros when the probe is off.
+void bso_get_probe(void * h, float * out)
+{
+    const auto * s = static_cast<const Sim *>(h);
+    const float v[6] = {s->probe.pos.x, s->probe.pos.y, s->probe.pos.z, s->probe.vel.x, s->probe.vel.y, s->probe.vel.z};
+    for (int k = 0; k < 6; ++k)
+        out[k] = s->probe_on ? v[k] : 0.0f;
 }
 
 void bso_destroy(void * h) { delete static_cast<Sim *>(h); }

@@ -68,6 +68,7 @@ def _bind(lib, prefix: str, cfg_type):
         "get_pairs": (C.c_int64, [C.c_void_p, C.c_int32, _i64p, C.c_int64]),
         "get_cells": (C.c_int, [C.c_void_p, C.c_int32, _i64p]),
     }
+    sig["get_probe"] = (None, [C.c_void_p, _f32p])
     if prefix == "bso_":
         sig["set_rigid_bodies"] = (C.c_int, [C.c_void_p, C.c_int32, _i32p, _i32p])
         sig["set_velocities"] = (None, [C.c_void_p, _f32p])
@@ -146,6 +147,11 @@ class _CpuSim:
     def _get3(self, name):
         out = np.zeros((self.n, 3), np.float32)
         self._fns[name](self.h, _p(out, C.c_float))
+        return out
+
+    def probe(self):
+        out = np.zeros(6, np.float32)
+        self._fns["get_probe"](self.h, _p(out, C.c_float))
         return out
 
     def positions(self):

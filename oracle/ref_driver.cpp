@@ -57,6 +57,7 @@ struct RefSim
     spn::SpringNetwork sn;
     cfgns::Configuration conf;
     bool rigid = false;
+    unsigned n = 0; // the caller's particles (the probe, when enabled, is appended after them)
 };
 
 cfgns::Configuration to_reference_config(const bs_config & c)
@@ -89,6 +90,16 @@ cfgns::Configuration to_reference_config(const bs_config & c)
     conf.viscosity.enable = c.viscosity_enable != 0;
     conf.viscosity.value = c.viscosity_value;
     conf.rigidbody.enable = c.rigidbody_enable != 0;
+    conf.probe.enable = c.probe_enable != 0;
+    conf.probe.enableelectrostatic = c.probe_electrostatic != 0;
+    conf.probe.enablesteric = c.probe_steric != 0;
+    conf.probe.x = c.probe_x;
+    conf.probe.y = c.probe_y;
+    conf.probe.z = c.probe_z;
+    conf.probe.mass = c.probe_mass;
+    conf.probe.epsilon = c.probe_epsilon;
+    conf.probe.radius = c.probe_radius;
+    conf.probe.charge = c.probe_charge;
     return conf;
 }
 
@@ -102,6 +113,7 @@ void * bsref_create(const bs_config * cfg, int64_t n, const float * xyz, const f
                     const int32_t * ij, const float * r0, const float * k)
 {
     auto * h = new RefSim();
+    h->n = static_cast<unsigned>(n);
     for (int64_t i = 0; i < n; ++i)
     {
         spn::Particle p;
@@ -172,7 +184,7 @@ double bsref_time_steps(void * hp, int nsteps)
 int bsref_compute_forces(void * hp)
 {
     auto * h = static_cast<RefSim *>(hp);
-    for (unsigned i = 0; i < h->sn.getNumberOfParticles(); ++i)
+    for (unsigned i = 0; i < h->n; ++i)
         h->sn.getParticle(i).resetForce();
     h->sn.idleRun();
     h->sn.computeForces();
@@ -182,7 +194,7 @@ int bsref_compute_forces(void * hp)
 void bsref_get_positions(void * hp, float * out)
 {
     auto * h = static_cast<RefSim *>(hp);
-    for (unsigned i = 0; i < h->sn.getNumberOfParticles(); ++i)
+    for (unsigned i = 0; i < h->n; ++i)
     {
         const Vector3f v = h->sn.getParticle(i).getPosition();
         out[3 * i] = v.getX();
@@ -194,7 +206,7 @@ void bsref_get_positions(void * hp, float * out)
 void bsref_get_velocities(void * hp, float * out)
 {
     auto * h = static_cast<RefSim *>(hp);
-    for (unsigned i = 0; i < h->sn.getNumberOfParticles(); ++i)
+    for (unsigned i = 0; i < h->n; ++i)
     {
         const Vector3f v = h->sn.getParticle(i).getVelocity();
         out[3 * i] = v.getX();
@@ -206,7 +218,7 @@ void bsref_get_velocities(void * hp, float * out)
 void bsref_get_forces(void * hp, float * out)
 {
     auto * h = static_cast<RefSim *>(hp);
-    for (unsigned i = 0; i < h->sn.getNumberOfParticles(); ++i)
+    for (unsigned i = 0; i < h->n; ++i)
     {
         const Vector3f v = h->sn.getParticle(i).getForce();
         out[3 * i] = v.getX();
@@ -221,9 +233,27 @@ void bsref_get_forces(void * hp, float * out)
 void bsref_set_positions(void * hp, const float * xyz)
 {
     auto * h = static_cast<RefSim *>(hp);
-    for (unsigned i = 0; i < h->sn.getNumberOfParticles(); ++i)
+    for (unsigned i = 0; i < h->n; ++i)
         h->sn.getParticle(i).setPosition(Vector3f(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]));
     h->sn.setup(h->conf);
+}
+
+// Probe position and velocity (the copy the reference keeps after the particles).
+void bsref_get_probe(void * hp, float * out)
+{
+    auto * h = static_cast<RefSim *>(hp);
+    for (int k = 0; k < 6; ++k)
+        out[k] = 0.0f;
+    if (!h->conf.probe.enable || h->sn.getNumberOfParticles() <= h->n)
+        return;
+    const auto & pr = h->sn.getProbeParticle();
+    const Vector3f x = pr.getPosition(), v = pr.getVelocity();
+    out[0] = x.getX();
+    out[1] = x.getY();
+    out[2] = x.getZ();
+    out[3] = v.getX();
+    out[4] = v.getY();
+    out[5] = v.getZ();
 }
 
 void bsref_get_energies(void * hp, double * out)

@@ -21,6 +21,11 @@ Fixtures:
                   SpringNetwork.cpp:281-292): positions after 20 steps
   nsearch.npz     1000 random particles in [-100, 100]^3, steric cutoff 10: the neighbour pairs
                   (src/tests/test-nsearch.cpp:103-129)
+  probe.npz       a charged 300-particle network with LJ 12-6 Amber and Coulomb, and the probe
+                  particle (probe.*, SpringNetwork.cpp:156-182) steric and electrostatic on:
+                  positions, probe state and energies after 1, 10 and 30 steps
+
+Usage: python tests/golden/make_golden.py [fixture ...]   (default: all; names without .npz)
 """
 
 from __future__ import annotations
@@ -170,6 +175,35 @@ def make_rigid() -> dict:
     return out
 
 
+def probe_system() -> W.System:
+    s = W.ca_network(n=300, seed=5)
+    rng = np.random.default_rng(3)
+    s.charge = np.where(rng.random(s.n) < 0.3, rng.choice([-1.0, 1.0], s.n), 0.0).astype(np.float32)
+    s.radius = rng.uniform(1.5, 2.0, s.n).astype(np.float32)
+    s.epsilon = rng.uniform(0.2, 0.5, s.n).astype(np.float32)
+    s.config.update(steric_mode=1, coulomb_enable=1, coulomb_cutoff=12.0, coulomb_dielectric=4.0,
+                    probe_enable=1, probe_steric=1, probe_electrostatic=1, probe_x=2.0, probe_y=-1.0,
+                    probe_z=3.0, probe_charge=1.0, probe_radius=2.5, probe_epsilon=0.8, probe_mass=5.0,
+                    timestep=0.05)
+    return s
+
+
+def make_probe() -> dict:
+    s = probe_system()
+    out: dict = {}
+    system_arrays("in_", s, out)
+    ref = po.Reference(s)
+    done = 0
+    for mark in (1, 10, 30):
+        ref.step(mark - done)
+        done = mark
+        out[f"pos_{mark}"] = ref.positions()
+        out[f"probe_{mark}"] = ref.probe()
+        out[f"energy_{mark}"] = ref.energies()
+    ref.close()
+    return out
+
+
 def make_nsearch() -> dict:
     rng = np.random.default_rng(1000)
     xyz = rng.uniform(-100, 100, size=(1000, 3)).astype(np.float32)
@@ -188,14 +222,18 @@ def main() -> None:
     build.build_synth()
     if not po.build_reference():
         raise SystemExit("the reference sources are not present: cannot generate golden fixtures")
-    scans: dict = {}
-    make_scans(scans)
-    np.savez_compressed(os.path.join(HERE, "scans.npz"), **scans)
-    np.savez_compressed(os.path.join(HERE, "ca300.npz"), **make_ca300())
+    makers = {"scans": None, "ca300": make_ca300, "rigid1": make_rigid, "nsearch": make_nsearch,
+              "probe": make_probe}
     for mode in range(4):
-        np.savez_compressed(os.path.join(HERE, f"mixed_m{mode}.npz"), **make_mixed(mode))
-    np.savez_compressed(os.path.join(HERE, "rigid1.npz"), **make_rigid())
-    np.savez_compressed(os.path.join(HERE, "nsearch.npz"), **make_nsearch())
+        makers[f"mixed_m{mode}"] = (lambda m: (lambda: make_mixed(m)))(mode)
+    wanted = sys.argv[1:] or list(makers)
+    for name in wanted:
+        if name == "scans":
+            scans: dict = {}
+            make_scans(scans)
+            np.savez_compressed(os.path.join(HERE, "scans.npz"), **scans)
+        else:
+            np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **makers[name]())
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

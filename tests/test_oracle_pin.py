@@ -144,3 +144,18 @@ def test_fp64_evaluator_close_to_reference_arithmetic():
     e32 = orc.energies()
     for k in (2, 3, 4):
         assert abs(e32[k] - e64[k]) <= 1e-5 * abs(e64[k]) + 1e-6
+
+
+def test_probe_particle():
+    """The probe (SpringNetwork.cpp:156-182): every dynamic particle against one extra particle,
+    steric and electrostatic, no cutoff; the probe integrates alone after the particle loop."""
+    g = load_golden("probe.npz")
+    s = system_from_golden(g)
+    orc = po.Oracle(s)
+    done = 0
+    for mark in (1, 10, 30):
+        orc.step(mark - done)
+        done = mark
+        same(orc.positions(), g[f"pos_{mark}"])
+        same(orc.probe(), g[f"probe_{mark}"])
+        same(orc.energies(), g[f"energy_{mark}"])

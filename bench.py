@@ -411,6 +411,61 @@ def run_adjoint(reps: int = 5) -> dict:
     }
 
 
+def run_case(name: str) -> dict:
+    """Small fixed drivers for profiling one kernel family (used by the ncu commands recorded
+    under profiles/): each sets up one workload, runs a few warm-up steps and then the launches
+    to capture."""
+    import torch
+    from biospring_gb300 import SpringNetwork, workloads as W
+
+    if name == "step100k":
+        system = make_workload()
+        net = SpringNetwork()
+        net.addParticles(**{k: v for k, v in system.arrays().items() if v is not None})
+        net.addSprings(system.ij, system.r0, system.k)
+        net.setup(system.bs_config())
+        net.computeStep(50)
+        stream = torch.cuda.ExternalStream(net.stream())
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        with torch.cuda.stream(stream):
+            e[0].record(stream)
+            for _ in range(20):
+                net.launchPhase(0)
+            e[1].record(stream)
+            e[2].record(stream)
+            for _ in range(50):
+                net.launchPhase(1)
+            e[3].record(stream)
+        torch.cuda.synchronize()
+        net.synchronize()
+        out = {"case": name, "rebuild_us": e[0].elapsed_time(e[1]) * 1000 / 20,
+               "step_us": e[2].elapsed_time(e[3]) * 1000 / 50}
+        net.close()
+        return out
+    if name == "batch64":
+        ens = W.ensemble(W.ensemble_sizes(count=64, seed=7), seed=11)
+        net = SpringNetwork()
+        net.addParticles(xyz=ens.xyz)
+        net.addSprings(ens.ij, ens.r0, ens.k)
+        net.setSystems(ens.meta["offsets"])
+        net.setBatchShape(512, 2, 4)
+        net.setup(ens.bs_config())
+        net.computeStep(2 * REBUILD)
+        net.close()
+        return {"case": name, "particles": int(ens.n), "systems": 64}
+    if name == "adjoint10k":
+        s, target, _ = W.adjoint_fit(10_000, seed=4)
+        s.config["precise_positions"] = 1
+        net = SpringNetwork()
+        net.addParticles(**{k: v for k, v in s.arrays().items() if v is not None})
+        net.addSprings(s.ij, s.r0, s.k)
+        net.setup(s.bs_config())
+        loss, _, _ = net.adjoint(40, target, 20)
+        net.close()
+        return {"case": name, "loss": loss}
+    raise SystemExit(f"unknown case {name}")
+
+
 def cpu_baseline(system, seconds: float = 15.0) -> dict:
     """The CPU restatement of the reference step on all host cores (OpenMP), bounded sample."""
     from oracle import pyoracle
@@ -463,7 +518,15 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and adjoint figures")
+    ap.add_argument("--case", choices=["step100k", "batch64", "adjoint10k"],
+                    help="run one small profiling driver instead of the benchmark")
     args = ap.parse_args()
+    if args.case:
+        from biospring_gb300 import build
+        if not os.path.exists(build.LIB):
+            build.build_all()
+        print(json.dumps(run_case(args.case)))
+        return
     if args.impl == "reference":
         if args.steps > 20:
             args.steps = 10  # a bounded CPU sample (each step is ~1 s of CPU work)

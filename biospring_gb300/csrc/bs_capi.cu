@@ -1066,7 +1066,9 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     p.imp_on = c.impala_enable != 0;
     p.visc_on = c.viscosity_enable != 0;
     p.steric_mode = c.steric_mode;
-    p.step_lanes = 4;
+    // lanes per particle: 8 for systems too small to fill the GPU with 4 (fewer than ~150 blocks
+    // of 128 threads per 100 SMs), else 4; BS_STEP_LANES overrides
+    p.step_lanes = n < 40000 ? 8 : 4;
     if (const char *env = std::getenv("BS_STEP_LANES"))
     {
         const int v = std::atoi(env);

@@ -117,6 +117,22 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x: float, dist=None, device: str = "cpu") -> float:
+    """The slowest rank's time: replicas run in parallel, the job ends with the last one."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(n: int, steps: int, slowest_ms: float, world: int) -> float:
+    """Whole-job particle-steps/s of `world` independent replicas of n particles (no exchange:
+    the plain path does not shard, each GPU steps its own system)."""
+    return world * n * steps / (slowest_ms * 1e-3)
+
+
 def make_workload(seed: int = 42):
     from biospring_gb300 import workloads as W
     return W.uniform_lj(n=N_PARTICLES, box=BOX, seed=seed, dielectric_mode=1, rebuild_every=REBUILD,
@@ -191,12 +207,8 @@ def run_native(args) -> dict:
         raise RuntimeError(f"timed region completed {done} of {steps} steps (a stale list forced a redo)")
     step_ms = [ev[i][0].elapsed_time(ev[i][2]) for i in range(steps)]
     kern_ms = [ev[i][1].elapsed_time(ev[i][2]) for i in range(steps)]
-    total_ms = float(sum(step_ms))
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * system.n * steps / (total_ms * 1e-3)
+    total_ms = max_over_ranks(float(sum(step_ms)), dist, "cuda")
+    value = replica_throughput(system.n, steps, total_ms, world)
 
     # warm, continuous throughput (graph-captured periods, no flush), for context
     torch.cuda.synchronize()

@@ -214,15 +214,32 @@ __device__ __forceinline__ void spring_forces(const Params &p, int s, int t, flo
                                               float &e)
 {
     const int deg = p.se_deg[s];
+    if (t >= deg)
+        return;
     const size_t stride = static_cast<size_t>(p.npad);
+    // software-pipelined: the next entry and its partner position are loaded before this one is used
+    size_t at = static_cast<size_t>(t) * stride + s;
+    unsigned int cn = __ldg(&p.se_col[at]);
+    float kn = __ldg(&p.se_k[at]), rn = __ldg(&p.se_r0[at]);
+    float4 pn = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!(cn & kEntryInactive))
+        pn = __ldg(&pos[cn & kSlotMask]);
     for (int k = t; k < deg; k += T)
     {
-        const size_t at = static_cast<size_t>(k) * stride + s;
-        const unsigned int c = __ldg(&p.se_col[at]);
+        const unsigned int c = cn;
+        const float kk = kn, r0 = rn;
+        const float4 pj = pn;
+        if (k + T < deg)
+        {
+            at += static_cast<size_t>(T) * stride;
+            cn = __ldg(&p.se_col[at]);
+            kn = __ldg(&p.se_k[at]);
+            rn = __ldg(&p.se_r0[at]);
+            if (!(cn & kEntryInactive))
+                pn = __ldg(&pos[cn & kSlotMask]);
+        }
         if (c & kEntryInactive)
             continue;
-        const float4 pj = __ldg(&pos[c & kSlotMask]);
-        const float kk = __ldg(&p.se_k[at]), r0 = __ldg(&p.se_r0[at]);
         const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         const float inv = r2 > 0.0f ? rsqrt_nr(r2) : 0.0f;
@@ -241,7 +258,7 @@ __device__ __forceinline__ void spring_forces(const Params &p, int s, int t, flo
 // KIND 0: list 0 in 16-bit mode (partner = slot + offset, dynamic partners, half the pair
 // energy); KIND 1: list 0 in 32-bit mode; KIND 2: list 3 (static partners, full energy).
 // The loop is software-pipelined: entries are loaded two iterations ahead of use and
-// positions one iteration ahead.
+// positions (and the LJ factor of the partner) one iteration ahead.
 template <int SM, int T, int KIND>
 __device__ __forceinline__ void steric_forces(const Params &p, int s, int t, float4 pi, float fhi_i,
                                               const float4 *__restrict__ pos, const float *__restrict__ fhi,
@@ -261,18 +278,24 @@ __device__ __forceinline__ void steric_forces(const Params &p, int s, int t, flo
     };
     const float lo2 = p.lo2_s, hi2 = p.hi2_s;
     const float w = KIND == 2 ? 1.0f : 0.5f;
+    constexpr bool LJ = SM != BS_STERIC_LINEAR;
     int jn = entry(t);
     int jn2 = t + T < cnt ? entry(t + T) : 0;
     float4 pn = __ldg(&pos[jn]);
+    float hn = LJ ? __ldg(&fhi[jn]) : 0.0f;
     for (int k = t; k < cnt; k += T)
     {
-        const int j = jn;
         const float4 pj = pn;
+        const float hj = hn;
         jn = jn2;
         if (k + 2 * T < cnt)
             jn2 = entry(k + 2 * T);
         if (k + T < cnt)
+        {
             pn = __ldg(&pos[jn]);
+            if (LJ)
+                hn = __ldg(&fhi[jn]);
+        }
         const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (r2 >= hi2)
@@ -301,7 +324,6 @@ __device__ __forceinline__ void steric_forces(const Params &p, int s, int t, flo
             const float inv2 = recip_nr(r2);
             const float i6 = inv2 * inv2 * inv2;
             const float t6 = pi.w * pj.w * i6;
-            const float hj = __ldg(&fhi[j]);
             float fod;
             if (SM == BS_STERIC_LJ_12_6_AMBER)
             {
@@ -339,10 +361,26 @@ __device__ __forceinline__ void coulomb_forces(const Params &p, int s, int t, fl
     const int cnt = L.cnt[s];
     const unsigned int *__restrict__ row = L.idx + static_cast<size_t>(s) * L.cap;
     const bool dist = p.dielectric_mode == BS_DIELECTRIC_DISTANCE;
+    if (t >= cnt)
+        return;
+    // software-pipelined like the steric loop: entries two ahead, partner data one ahead
+    unsigned int jn = __ldg(row + t);
+    unsigned int jn2 = t + T < cnt ? __ldg(row + t + T) : 0u;
+    float4 pn = __ldg(&pos[jn & kSlotMask]);
+    float qn = __ldg(&chg[jn & kSlotMask]);
     for (int k = t; k < cnt; k += T)
     {
-        const unsigned int j = __ldg(row + k);
-        const float4 pj = __ldg(&pos[j & kSlotMask]);
+        const unsigned int j = jn;
+        const float4 pj = pn;
+        const float qj = qn;
+        jn = jn2;
+        if (k + 2 * T < cnt)
+            jn2 = __ldg(row + k + 2 * T);
+        if (k + T < cnt)
+        {
+            pn = __ldg(&pos[jn & kSlotMask]);
+            qn = __ldg(&chg[jn & kSlotMask]);
+        }
         const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (!pair_in(r2, p.lo2_c, p.hi2_c, pi, pj, p.c_coulomb, true))
@@ -350,7 +388,7 @@ __device__ __forceinline__ void coulomb_forces(const Params &p, int s, int t, fl
         if (r2 < 1e-6f) // d < 0.001 A gives zero (electrostatic.hpp:18-19)
             continue;
         const float inv = rsqrt_nr(r2);
-        const float qq = qi * __ldg(&chg[j & kSlotMask]);
+        const float qq = qi * qj;
         const float w = (j & kEntryStatic) ? 1.0f : 0.5f;
         float tq = qq * inv;
         float fod;

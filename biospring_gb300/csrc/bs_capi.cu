@@ -844,7 +844,9 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     BS_CUDA(s->dev.alloc(&p.cell_of, npad));
     BS_CUDA(s->dev.alloc(&p.tmp_perm, npad));
     s->step_blocks = static_cast<int>((static_cast<long long>(p.n) * 8 + kStepBlock - 1) / kStepBlock);
-    BS_CUDA(s->dev.alloc(&p.blk_energy, static_cast<size_t>(s->step_blocks) * 8));
+    p.blk_cap = s->step_blocks;
+    BS_CUDA(s->dev.alloc(&p.blk_energy, energy_scratch_doubles(s->step_blocks)));
+    BS_CUDA(cudaMemsetAsync(p.blk_energy, 0, sizeof(double) * energy_scratch_doubles(s->step_blocks), s->stream));
     BS_CUDA(s->dev.alloc(&p.ctl, 1));
     BS_CUDA(s->dev.alloc(&s->staging, 3 * static_cast<size_t>(n)));
     BS_CUDA(cudaMallocHost(reinterpret_cast<void **>(&s->ctl_host), sizeof(Ctl)));

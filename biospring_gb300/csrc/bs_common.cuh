@@ -62,6 +62,15 @@ constexpr int kTerms = 3; // nonbonded terms: steric, Coulomb, hydrophobic
 constexpr int kLists = 4;
 constexpr int kListStericStatic = 3;
 
+// Step energies are reduced block -> group of kEnergyGroup blocks -> grid; the scratch holds
+// 16 floats per block partial and per group partial, then one counter per group.
+constexpr int kEnergyGroup = 32;
+__host__ __device__ constexpr int energy_groups(int blocks) { return (blocks + kEnergyGroup - 1) / kEnergyGroup; }
+__host__ __device__ constexpr size_t energy_scratch_doubles(int blocks)
+{
+    return static_cast<size_t>(blocks + energy_groups(blocks)) * 8 + (energy_groups(blocks) + 1) / 2;
+}
+
 // Device control block: one per simulation handle, in device memory.
 struct Ctl
 {
@@ -175,7 +184,8 @@ struct Params
     int *tile_sum;            // [cell_cap / kScanTile + 2] per-tile totals of the cell scan
     int pl_sparse;            // build the pair lists one warp per particle (few particles per cell)
     // energies: per-block partials
-    double *blk_energy;       // [step blocks * 8]
+    double *blk_energy;       // block and group partials of the step energies, group counters
+    int blk_cap;              // block partials it holds (the step kernel's largest grid)
     Ctl *ctl;
     // configuration
     float dt;

@@ -130,15 +130,40 @@ __device__ __forceinline__ void ff_add(float &hi, float &lo, float h2, float l2)
     two_sum(s, e, hi, lo);
 }
 
-// Deterministic reduction of NE per-thread float partials over the grid. Warp sums are FP32
-// trees, block sums float-float (compensated), the block partials are stored as (hi, lo) pairs, and the
-// last block to finish sums them in block order, also float-float, and writes the totals as
-// double. The result carries the accuracy of an FP64 reduction without using the FP64 pipe,
-// which runs at a small fraction of the FP32 rate on this part.
-template <int NE, int BLOCK>
-__device__ __forceinline__ bool reduce_energies(const float (&e)[NE], double *blk_d, unsigned int *done, double *dst)
+// Deterministic reduction of NE per-thread float partials over the grid, in three levels:
+// block -> group of kEnergyGroup consecutive blocks -> grid. Warp sums are FP32 trees; above the
+// warp every sum is float-float (compensated, about 44 significant bits). The last block of a
+// group to finish sums the group's block partials, and the last group to finish sums the group
+// partials and writes the totals as double. Every sum runs in a fixed order (lane = block or
+// group index, a fixed shuffle tree), so the result does not depend on which block finishes
+// last. The group level keeps the serial tail short: the final block reads a few hundred
+// partials instead of one per block of the grid. The result carries the accuracy of an FP64
+// reduction without the FP64 pipe, which runs at a small fraction of the FP32 rate on this part.
+//
+// blk_d holds [blk_cap][16] floats of block partials ((hi, lo) per energy), then
+// [energy_groups(blk_cap)][16] floats of group partials, then one counter per group; the
+// counters and *done start at zero and are reset by the block that completes them.
+// (hi, lo) of lane `lane` summed over the warp in a fixed tree; the total lands in lane 0.
+__device__ __forceinline__ void warp_ff_sum(float &hi, float &lo)
 {
-    float *blk = reinterpret_cast<float *>(blk_d); // [block][16]: (hi, lo) per energy
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
+        const float l2 = __shfl_down_sync(0xffffffffu, lo, o);
+        ff_add(hi, lo, h2, l2);
+    }
+}
+
+template <int NE, int BLOCK>
+__device__ __forceinline__ bool reduce_energies(const float (&e)[NE], double *blk_d, int blk_cap, unsigned int *done,
+                                                double *dst)
+{
+    static_assert(NE <= 8, "16 floats per partial");
+    float *blk = reinterpret_cast<float *>(blk_d);
+    float *grp = blk + static_cast<size_t>(blk_cap) * 16;
+    const int ngrp = energy_groups(gridDim.x);
+    unsigned int *grp_cnt = reinterpret_cast<unsigned int *>(grp + static_cast<size_t>(energy_groups(blk_cap)) * 16);
     __shared__ float shh[NE][BLOCK / 32], shl[NE][BLOCK / 32];
     __shared__ bool am_last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -165,42 +190,59 @@ __device__ __forceinline__ bool reduce_energies(const float (&e)[NE], double *bl
         blk[static_cast<size_t>(blockIdx.x) * 16 + 2 * threadIdx.x] = hi;
         blk[static_cast<size_t>(blockIdx.x) * 16 + 2 * threadIdx.x + 1] = lo;
     }
+    // ---- group level: the last block of the group sums its kEnergyGroup block partials ----
+    const int g = blockIdx.x / kEnergyGroup;
+    const int g0 = g * kEnergyGroup;
+    const int gsize = min(kEnergyGroup, static_cast<int>(gridDim.x) - g0);
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0)
-        am_last = atomicAdd(done, 1u) == gridDim.x - 1;
+        am_last = atomicAdd(&grp_cnt[g], 1u) == static_cast<unsigned int>(gsize - 1);
     __syncthreads();
     if (!am_last)
         return false;
     __threadfence();
-    for (int k = 0; k < NE; ++k)
+    for (int k = warp; k < NE; k += BLOCK / 32)
     {
         float hi = 0.0f, lo = 0.0f;
-        for (unsigned int b = threadIdx.x; b < gridDim.x; b += BLOCK)
-            ff_add(hi, lo, __ldcg(&blk[static_cast<size_t>(b) * 16 + 2 * k]),
-                   __ldcg(&blk[static_cast<size_t>(b) * 16 + 2 * k + 1]));
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
+        if (lane < gsize)
         {
-            const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
-            const float l2 = __shfl_down_sync(0xffffffffu, lo, o);
-            ff_add(hi, lo, h2, l2);
+            const float2 v = __ldcg(reinterpret_cast<const float2 *>(blk + static_cast<size_t>(g0 + lane) * 16 + 2 * k));
+            hi = v.x;
+            lo = v.y;
         }
-        __syncthreads();
+        warp_ff_sum(hi, lo);
         if (lane == 0)
         {
-            shh[0][warp] = hi;
-            shl[0][warp] = lo;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0)
-        {
-            float th = 0.0f, tl = 0.0f;
-            for (int w = 0; w < BLOCK / 32; ++w)
-                ff_add(th, tl, shh[0][w], shl[0][w]);
-            dst[k] = static_cast<double>(th) + static_cast<double>(tl);
+            grp[static_cast<size_t>(g) * 16 + 2 * k] = hi;
+            grp[static_cast<size_t>(g) * 16 + 2 * k + 1] = lo;
         }
     }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        grp_cnt[g] = 0u;
+        am_last = atomicAdd(done, 1u) == static_cast<unsigned int>(ngrp - 1);
+    }
+    __syncthreads();
+    if (!am_last)
+        return false;
+    __threadfence();
+    // ---- grid level: lane l sums groups l, l + 32, ... in order, then a fixed warp tree ----
+    for (int k = warp; k < NE; k += BLOCK / 32)
+    {
+        float hi = 0.0f, lo = 0.0f;
+        for (int q = lane; q < ngrp; q += 32)
+        {
+            const float2 v = __ldcg(reinterpret_cast<const float2 *>(grp + static_cast<size_t>(q) * 16 + 2 * k));
+            ff_add(hi, lo, v.x, v.y);
+        }
+        warp_ff_sum(hi, lo);
+        if (lane == 0)
+            dst[k] = static_cast<double>(hi) + static_cast<double>(lo);
+    }
+    __syncthreads();
     if (threadIdx.x == 0)
         *done = 0u;
     return true;
@@ -298,12 +340,13 @@ __device__ __forceinline__ void steric_forces(const Params &p, int s, int t, flo
         }
         const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 >= hi2)
-            continue;
-        if (!(r2 < lo2 && r2 > 1e-20f) && !exact_pair_test(pi, pj, p.c_steric, false))
-            continue;
         if (SM == BS_STERIC_LINEAR)
         {
+            // Few listed pairs overlap: the branches skip the square root and division of the rest.
+            if (r2 >= hi2)
+                continue;
+            if (!(r2 < lo2 && r2 > 1e-20f) && !exact_pair_test(pi, pj, p.c_steric, false))
+                continue;
             // steric.hpp:37-59: E = (d - (ri + rj))^2 / 2 when overlapping, |F| = |d - (ri + rj)|.
             // d - (ri + rj) cancels near contact, so d is the correctly rounded square root here.
             const float d = sqrtf(r2);
@@ -319,30 +362,38 @@ __device__ __forceinline__ void steric_forces(const Params &p, int s, int t, flo
         }
         else
         {
-            if (r2 < 0.01f) // d < 0.1 A: the LJ forms give zero (steric.hpp:71-72)
-                continue;
+            // Most listed pairs are inside the cutoff: the body is branch-free and a rejected
+            // entry adds exact zeros (selects, not products, so an infinite or NaN term of a
+            // rejected pair cannot leak in). Only entries inside the guard band, or
+            // (near-)coincident, branch to the exact reference test.
+            bool ok = r2 < lo2 && r2 > 1e-20f;
+            if (!ok && r2 < hi2)
+                ok = exact_pair_test(pi, pj, p.c_steric, false);
+            ok = ok && !(r2 < 0.01f); // d < 0.1 A: the LJ forms give zero (steric.hpp:71-72)
             const float inv2 = recip_nr(r2);
             const float i6 = inv2 * inv2 * inv2;
             const float t6 = pi.w * pj.w * i6;
-            float fod;
+            float fod, de;
             if (SM == BS_STERIC_LJ_12_6_AMBER)
             {
                 const float t12 = fhi_i * hj * i6 * i6;
-                e = fmaf(w, t12 - 2.0f * t6, e);
+                de = t12 - 2.0f * t6;
                 fod = 12.0f * (t6 - t12) * inv2;
             }
             else if (SM == BS_STERIC_LJ_8_6_LEWITT)
             {
                 const float t8 = fhi_i * hj * i6 * inv2;
-                e = fmaf(w, 3.0f * t8 - 4.0f * t6, e);
+                de = 3.0f * t8 - 4.0f * t6;
                 fod = 24.0f * (t6 - t8) * inv2;
             }
             else
             {
                 const float t8 = fhi_i * hj * i6 * inv2;
-                e = fmaf(w, t8 - t6, e);
+                de = t8 - t6;
                 fod = (6.0f * t6 - 8.0f * t8) * inv2;
             }
+            e = fmaf(w, ok ? de : 0.0f, e);
+            fod = ok ? fod : 0.0f;
             fx = fmaf(dx, fod, fx);
             fy = fmaf(dy, fod, fy);
             fz = fmaf(dz, fod, fz);

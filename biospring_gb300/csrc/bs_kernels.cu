@@ -608,7 +608,7 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
 // integrates. T > 1 gives the latency-bound gather loops T times more independent loads in
 // flight than one thread per particle would.
 template <int MODE, int SM, int T>
-__global__ void __launch_bounds__(kStepBlock, kStepMinBlocks) k_step(Params p)
+__global__ void __launch_bounds__(kStepKernelBlock, kStepMinBlocks) k_step(Params p)
 {
     Ctl *ctl = p.ctl;
     if (status_of(ctl) != 0)
@@ -619,7 +619,7 @@ __global__ void __launch_bounds__(kStepBlock, kStepMinBlocks) k_step(Params p)
     const int pend = particle_step<MODE, SM, T>(p, g / T, g % T, p.n, sb, lb, ctl->ext_pending != 0, e);
     if (pend)
         atomicOr(&ctl->status_pending, pend);
-    if (reduce_energies<6, kStepBlock>(e, p.blk_energy, &ctl->done_step, ctl->energies))
+    if (reduce_energies<6, kStepKernelBlock>(e, p.blk_energy, p.blk_cap, &ctl->done_step, ctl->energies))
     {
         if (threadIdx.x == 0)
         {
@@ -951,20 +951,20 @@ template <int MODE, int SM>
 static void launch_step_lanes(const Params &p, cudaStream_t st)
 {
     const long long threads_per = p.step_lanes;
-    const int nb = static_cast<int>((static_cast<long long>(p.n) * threads_per + kStepBlock - 1) / kStepBlock);
+    const int nb = static_cast<int>((static_cast<long long>(p.n) * threads_per + kStepKernelBlock - 1) / kStepKernelBlock);
     switch (p.step_lanes)
     {
     case 1:
-        k_step<MODE, SM, 1><<<nb, kStepBlock, 0, st>>>(p);
+        k_step<MODE, SM, 1><<<nb, kStepKernelBlock, 0, st>>>(p);
         break;
     case 2:
-        k_step<MODE, SM, 2><<<nb, kStepBlock, 0, st>>>(p);
+        k_step<MODE, SM, 2><<<nb, kStepKernelBlock, 0, st>>>(p);
         break;
     case 8:
-        k_step<MODE, SM, 8><<<nb, kStepBlock, 0, st>>>(p);
+        k_step<MODE, SM, 8><<<nb, kStepKernelBlock, 0, st>>>(p);
         break;
     default:
-        k_step<MODE, SM, 4><<<nb, kStepBlock, 0, st>>>(p);
+        k_step<MODE, SM, 4><<<nb, kStepKernelBlock, 0, st>>>(p);
         break;
     }
 }

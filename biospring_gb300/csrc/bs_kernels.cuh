@@ -6,11 +6,16 @@
 namespace bsg
 {
 
-constexpr int kStepBlock = 128;
-#ifndef BS_STEP_MIN_BLOCKS
-#define BS_STEP_MIN_BLOCKS 8
+constexpr int kStepBlock = 128; // adjoint and diagnostic kernels
+#ifndef BS_STEP_BLOCK
+#define BS_STEP_BLOCK 256
 #endif
-// resident blocks of 128 threads per SM the step kernel is compiled for (8: at most 64 registers)
+#ifndef BS_STEP_MIN_BLOCKS
+#define BS_STEP_MIN_BLOCKS (1024 / BS_STEP_BLOCK)
+#endif
+// threads per block of the step kernel, and the resident blocks per SM it is compiled for
+// (1024 resident threads: at most 64 registers)
+constexpr int kStepKernelBlock = BS_STEP_BLOCK;
 constexpr int kStepMinBlocks = BS_STEP_MIN_BLOCKS;
 constexpr int kBuildBlock = 128;
 constexpr int kBuildLanes = 8;    // lanes sharing one particle in the pair-list build

@@ -397,7 +397,9 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
     constexpr int kRuns = (2 * kGridDiv + 1) * (2 * kGridDiv + 1);
     __shared__ int sh_run[kRuns][3]; // first slot, end slot, offset in the stage
     __shared__ float4 sh_pos[kPlStage];
-    __shared__ int blocked, staged;
+    __shared__ int sh_slot[kPlStage];
+    __shared__ unsigned char sh_flag[kPlStage];
+    __shared__ int blocked, staged, staged_tot;
     Ctl *ctl = p.ctl;
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nx = ctl->gnx, ny = ctl->gny, nz = ctl->gnz;
@@ -442,6 +444,7 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
             }
         }
         staged = tot <= kPlStage;
+        staged_tot = tot;
         // every candidate offset of this cell fits 16 bits, or the list goes 32-bit
         if (PL16 && (hi - 1 - h0 > 32767 || lo - (h1 - 1) < -32768))
             atomicOr(&ctl->status, ST_WIDE);
@@ -453,7 +456,11 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
         {
             const int j0 = sh_run[r][0], len = sh_run[r][1] - j0, o = sh_run[r][2];
             for (int k = threadIdx.x; k < len; k += blockDim.x)
+            {
                 sh_pos[o + k] = p.pos[ctl->sbuf][j0 + k];
+                sh_slot[o + k] = j0 + k;
+                sh_flag[o + k] = static_cast<unsigned char>(p.flags[ctl->lbuf][j0 + k]);
+            }
         }
     __syncthreads();
     const int sb = ctl->sbuf, lb = ctl->lbuf;
@@ -511,77 +518,92 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
             unsigned int *row1 = p.pl[1].idx + static_cast<size_t>(i) * cap1;
             unsigned int *row2 = p.pl[2].idx + static_cast<size_t>(i) * cap2;
             unsigned int *row3 = p.pl[3].idx + static_cast<size_t>(i) * cap3;
-            for (int r = 0; r < kRuns; ++r)
-            {
-                const int j0 = sh_run[r][0], j1 = sh_run[r][1];
-                const float4 *src = staged ? sh_pos + sh_run[r][2] - j0 : pos;
-                for (int jb = j0; jb < j1; jb += 32)
+            // One window of up to 32 candidates, one per lane. Each lane sees its candidates in
+            // ascending slot order over the windows, so it walks the sorted spring partners with
+            // its own pointer bp (at most deg steps over the whole scan).
+            auto window = [&](const int j, const bool jv, const float4 pj, const unsigned int fj) {
+                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                bool in = jv && r2 < r2max && j != i;
+                if (deg)
                 {
-                    const int j = jb + lane;
-                    const bool jv = j < j1;
-                    const int jc = jv ? j : j1 - 1;
-                    const float4 pj = src[jc];
-                    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                    const float r2 = dx * dx + dy * dy + dz * dz;
-                    bool in = jv && r2 < r2max && j != i;
-                    if (deg)
+                    if (small)
                     {
-                        if (small)
-                        {
-                            while (bp < deg && part[bp] < jb)
-                                ++bp;
-                            for (int k = bp; k < deg && part[k] < jb + 32; ++k)
-                                in = in && part[k] != j;
-                        }
-                        else
-                            for (int k = 0; k < deg; ++k)
-                                in = in && static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask) != j;
+                        while (bp < deg && part[bp] < j)
+                            ++bp;
+                        in = in && !(bp < deg && part[bp] == j);
                     }
-                    const unsigned int fj = need_fj ? fl[jc] : 0u;
-                    const bool st = (fj & PF_STATIC) != 0;
-                    if (on0)
+                    else
+                        for (int k = 0; k < deg; ++k)
+                            in = in && static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask) != j;
+                }
+                const bool st = (fj & PF_STATIC) != 0;
+                if (on0)
+                {
+                    const bool a0 = in && !st && r2 < r2_0;
+                    const unsigned int m0 = __ballot_sync(0xffffffffu, a0);
+                    if (a0)
                     {
-                        const bool a0 = in && !st && r2 < r2_0;
-                        const unsigned int m0 = __ballot_sync(0xffffffffu, a0);
-                        if (a0)
+                        const int at = cnt0 + __popc(m0 & below);
+                        if (at < cap0)
                         {
-                            const int at = cnt0 + __popc(m0 & below);
-                            if (at < cap0)
-                            {
-                                if (PL16)
-                                    row0s[at] = static_cast<short>(j - i);
-                                else
-                                    row0[at] = static_cast<unsigned int>(j);
-                            }
-                        }
-                        cnt0 += __popc(m0);
-                        if (l3)
-                        {
-                            const bool a3 = in && st && r2 < r2_0;
-                            const unsigned int m3 = __ballot_sync(0xffffffffu, a3);
-                            if (a3 && cnt3 + __popc(m3 & below) < cap3)
-                                row3[cnt3 + __popc(m3 & below)] = static_cast<unsigned int>(j) | kEntryStatic;
-                            cnt3 += __popc(m3);
+                            if (PL16)
+                                row0s[at] = static_cast<short>(j - i);
+                            else
+                                row0[at] = static_cast<unsigned int>(j);
                         }
                     }
-                    if (on1)
+                    cnt0 += __popc(m0);
+                    if (l3)
                     {
-                        const bool a1 = in && (fj & PF_CHARGED) && r2 < r2_1;
-                        const unsigned int m1 = __ballot_sync(0xffffffffu, a1);
-                        if (a1 && cnt1 + __popc(m1 & below) < cap1)
-                            row1[cnt1 + __popc(m1 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
-                        cnt1 += __popc(m1);
-                    }
-                    if (on2)
-                    {
-                        const bool a2 = in && (fj & PF_HYDROPHOBIC) && r2 < r2_2;
-                        const unsigned int m2 = __ballot_sync(0xffffffffu, a2);
-                        if (a2 && cnt2 + __popc(m2 & below) < cap2)
-                            row2[cnt2 + __popc(m2 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
-                        cnt2 += __popc(m2);
+                        const bool a3 = in && st && r2 < r2_0;
+                        const unsigned int m3 = __ballot_sync(0xffffffffu, a3);
+                        if (a3 && cnt3 + __popc(m3 & below) < cap3)
+                            row3[cnt3 + __popc(m3 & below)] = static_cast<unsigned int>(j) | kEntryStatic;
+                        cnt3 += __popc(m3);
                     }
                 }
+                if (on1)
+                {
+                    const bool a1 = in && (fj & PF_CHARGED) && r2 < r2_1;
+                    const unsigned int m1 = __ballot_sync(0xffffffffu, a1);
+                    if (a1 && cnt1 + __popc(m1 & below) < cap1)
+                        row1[cnt1 + __popc(m1 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
+                    cnt1 += __popc(m1);
+                }
+                if (on2)
+                {
+                    const bool a2 = in && (fj & PF_HYDROPHOBIC) && r2 < r2_2;
+                    const unsigned int m2 = __ballot_sync(0xffffffffu, a2);
+                    if (a2 && cnt2 + __popc(m2 & below) < cap2)
+                        row2[cnt2 + __popc(m2 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
+                    cnt2 += __popc(m2);
+                }
+            };
+            if (staged)
+            {
+                // the staged runs are one ascending sequence of slots: full windows across runs
+                const int tot = staged_tot;
+                for (int jb = 0; jb < tot; jb += 32)
+                {
+                    const int q = jb + lane;
+                    const bool jv = q < tot;
+                    const int qc = jv ? q : tot - 1;
+                    window(sh_slot[qc], jv, sh_pos[qc], sh_flag[qc]);
+                }
             }
+            else
+                for (int r = 0; r < kRuns; ++r)
+                {
+                    const int j0 = sh_run[r][0], j1 = sh_run[r][1];
+                    for (int jb = j0; jb < j1; jb += 32)
+                    {
+                        const int j = jb + lane;
+                        const bool jv = j < j1;
+                        const int jc = jv ? j : j1 - 1;
+                        window(jc, jv, pos[jc], need_fj ? fl[jc] : 0u);
+                    }
+                }
         }
         if (lane == 0)
         {

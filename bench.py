@@ -50,6 +50,7 @@ REBUILD = 10
 STEP_BYTES_PER_PARTICLE_BASE = 84.0   # positions r+w 32, velocities r+w 32, parameters 16, row pointer 4
 SPRING_BYTES_PER_ENTRY = 12.0         # partner index + stiffness + rest length
 REBUILD_BYTES_PER_PARTICLE = 104.0    # key 4 + permutation 4 + gather/scatter of x, v, parameters 3 x 32
+CTL_BYTES = 288                       # device control block (status, step count, energies) read per bs_step
 
 
 def peaks() -> dict:
@@ -263,9 +264,11 @@ def run_native(args) -> dict:
             "timing": "CUDA events on the library stream around each step (rebuild on every 10th)",
         },
         "gpu_launches": int(launches),
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(system.n * 16),
-                "d2h_bytes_per_step": 48,
-                "path": "bs_set_external_forces + bs_step(1) + bs_get_energies per step"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(system.n * 12 + 4),
+                "d2h_bytes_per_step": CTL_BYTES,
+                "path": "bs_set_external_forces (pinned float[3n], copied straight to the device) + "
+                        "bs_step(1) + bs_get_energies per step; the energies come with the control "
+                        "block bs_step reads back to check the step"},
         "roofline": {
             "bound": "hbm",
             "kernel": "k_step (forces + Euler step)",

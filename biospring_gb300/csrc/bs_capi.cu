@@ -64,8 +64,9 @@ struct bs_sim
     Params p{};
     Ctl *ctl_host = nullptr; // pinned mirror
     float *staging = nullptr; // device float[3n]
-    float4 *ext_host = nullptr; // pinned
-    bool ext_dirty = false;
+    float *ext_stage = nullptr; // pinned float[3n]: external forces from pageable caller memory
+    int *one_host = nullptr;    // pinned constant 1 (source of the ext_pending flag)
+    long long ctl_read_at = -1; // launch count when ctl_host was last read (all work finished)
     int step_blocks = 0;
     // schedule
     bool list_valid = false;
@@ -166,11 +167,17 @@ void release_device(bs_sim *s)
         cudaFreeHost(s->ctl_host);
         s->ctl_host = nullptr;
     }
-    if (s->ext_host)
+    if (s->ext_stage)
     {
-        cudaFreeHost(s->ext_host);
-        s->ext_host = nullptr;
+        cudaFreeHost(s->ext_stage);
+        s->ext_stage = nullptr;
     }
+    if (s->one_host)
+    {
+        cudaFreeHost(s->one_host);
+        s->one_host = nullptr;
+    }
+    s->ctl_read_at = -1;
     s->ready = false;
 }
 
@@ -186,6 +193,7 @@ int read_ctl(bs_sim *s)
 {
     BS_CUDA(cudaMemcpyAsync(s->ctl_host, s->p.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s->stream));
     BS_CUDA(cudaStreamSynchronize(s->stream));
+    s->ctl_read_at = s->launches;
     return BS_OK;
 }
 
@@ -247,23 +255,6 @@ int current_caps(const bs_sim *s, int caps[kLists])
     for (int t = 0; t < kLists; ++t)
         caps[t] = s->p.pl[t].cap;
     return 0;
-}
-
-int sync_ext(bs_sim *s)
-{
-    if (!s->ext_dirty)
-        return BS_OK;
-    BS_CUDA(cudaMemcpyAsync(s->p.ext, s->ext_host, sizeof(float4) * s->n, cudaMemcpyHostToDevice, s->stream));
-    int one = 1;
-    s->ctl_host->ext_pending = 1;
-    BS_CUDA(cudaMemcpyAsync(&s->p.ctl->ext_pending, &s->ctl_host->ext_pending, sizeof(int), cudaMemcpyHostToDevice,
-                            s->stream));
-    (void)one;
-    BS_CUDA(cudaStreamSynchronize(s->stream));
-    std::memset(s->ext_host, 0, sizeof(float4) * s->n);
-    s->ext_dirty = false;
-    // (the pinned buffer is reused for the next step's forces once the copy has completed)
-    return BS_OK;
 }
 
 // Runs a rebuild now and repairs capacity overflows until the list is valid.
@@ -822,7 +813,7 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
             BS_CUDA(s->dev.alloc(&p.pos_lo[b], npad));
             BS_CUDA(cudaMemsetAsync(p.pos_lo[b], 0, sizeof(float4) * npad, s->stream));
         }
-    BS_CUDA(s->dev.alloc(&p.ext, n));
+    BS_CUDA(s->dev.alloc(&p.ext, 3 * static_cast<size_t>(n)));
     BS_CUDA(s->dev.alloc(&p.force_out, n));
     int *d_row;
     unsigned int *d_col;
@@ -850,8 +841,9 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     BS_CUDA(s->dev.alloc(&p.ctl, 1));
     BS_CUDA(s->dev.alloc(&s->staging, 3 * static_cast<size_t>(n)));
     BS_CUDA(cudaMallocHost(reinterpret_cast<void **>(&s->ctl_host), sizeof(Ctl)));
-    BS_CUDA(cudaMallocHost(reinterpret_cast<void **>(&s->ext_host), sizeof(float4) * n));
-    std::memset(s->ext_host, 0, sizeof(float4) * n);
+    BS_CUDA(cudaMallocHost(reinterpret_cast<void **>(&s->ext_stage), sizeof(float) * 3 * n));
+    BS_CUDA(cudaMallocHost(reinterpret_cast<void **>(&s->one_host), sizeof(int)));
+    *s->one_host = 1;
 
     // ---- pair lists: which terms, radii, first capacities from the density ----
     const double skin = c.list_skin;
@@ -961,7 +953,7 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     BS_CUDA(cudaMemcpyAsync(d_col, col.data(), sizeof(int) * std::max(nnz, 1), cudaMemcpyHostToDevice, s->stream));
     BS_CUDA(cudaMemcpyAsync(d_k, kk.data(), sizeof(float) * std::max(nnz, 1), cudaMemcpyHostToDevice, s->stream));
     BS_CUDA(cudaMemcpyAsync(d_r0, rr.data(), sizeof(float) * std::max(nnz, 1), cudaMemcpyHostToDevice, s->stream));
-    BS_CUDA(cudaMemsetAsync(p.ext, 0, sizeof(float4) * n, s->stream));
+    BS_CUDA(cudaMemsetAsync(p.ext, 0, sizeof(float) * 3 * n, s->stream));
     BS_CUDA(cudaMemsetAsync(p.force_out, 0, sizeof(float4) * n, s->stream));
     std::memset(s->ctl_host, 0, sizeof(Ctl));
     for (int k = 0; k < 3; ++k)
@@ -1175,10 +1167,8 @@ int bs_step_async(bs_sim *s, int32_t nsteps)
         return fail(s, BS_E_STATE, "bs_step: call bs_setup first");
     if (nsteps < 0)
         return fail(s, BS_E_ARG, "bs_step: negative step count");
-    int rc = sync_ext(s);
-    if (rc)
-        return rc;
     s->target += nsteps;
+    int rc = BS_OK;
     if (s->p.nsys > 0)
         return enqueue_batch(s, nsteps, false);
     return enqueue_steps(s, nsteps);
@@ -1327,9 +1317,21 @@ int bs_set_external_forces(bs_sim *s, const float *f)
         return fail(s, BS_E_STATE, "external forces are not available for batched ensembles");
     if (!f)
         return fail(s, BS_E_ARG, "bs_set_external_forces: null forces");
-    for (int64_t i = 0; i < s->n; ++i)
-        s->ext_host[i] = make_float4(f[3 * i], f[3 * i + 1], f[3 * i + 2], 0.f);
-    s->ext_dirty = true;
+    // Copied at once, in stream order after the enqueued steps: straight from the caller's buffer
+    // when it is page-locked, else through the handle's pinned staging buffer. The call returns
+    // when the copy is done, so the caller may reuse f.
+    const size_t bytes = sizeof(float) * 3 * static_cast<size_t>(s->n);
+    cudaPointerAttributes attr{};
+    const bool pinned = cudaPointerGetAttributes(&attr, f) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+    if (!pinned)
+    {
+        cudaGetLastError(); // clear a pageable-pointer query error, if any
+        BS_CUDA(cudaStreamSynchronize(s->stream)); // the staging buffer may still feed an earlier copy
+        std::memcpy(s->ext_stage, f, bytes);
+    }
+    BS_CUDA(cudaMemcpyAsync(s->p.ext, pinned ? f : s->ext_stage, bytes, cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaMemcpyAsync(&s->p.ctl->ext_pending, s->one_host, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    BS_CUDA(cudaStreamSynchronize(s->stream));
     return BS_OK;
 }
 
@@ -1346,9 +1348,6 @@ int bs_compute_forces(bs_sim *s)
     if (!s->ready)
         return fail(s, BS_E_STATE, "bs_compute_forces: call bs_setup first");
     int rc = settle(s);
-    if (rc)
-        return rc;
-    rc = sync_ext(s);
     if (rc)
         return rc;
     if (!s->list_valid || (s->ctl_host->status & ST_STALE))
@@ -1423,10 +1422,9 @@ int bs_set_force(bs_sim *s, int64_t i, const float f[3])
         return fail(s, BS_E_STATE, "external forces are not available for batched ensembles");
     if (i < 0 || i >= s->n || !f)
         return fail(s, BS_E_ARG, "bs_set_force: particle index out of range");
-    s->ext_host[i].x += f[0];
-    s->ext_host[i].y += f[1];
-    s->ext_host[i].z += f[2];
-    s->ext_dirty = true;
+    // added on the device in stream order: applies to the next step (after any enqueued ones)
+    s->launches += launch_ext_add(s->p, i, f[0], f[1], f[2], s->stream);
+    BS_CUDA(cudaGetLastError());
     return BS_OK;
 }
 
@@ -1439,9 +1437,14 @@ int bs_get_energies(bs_sim *s, double out[BS_NUM_ENERGIES])
     const int rc = settle(s);
     if (rc)
         return rc;
-    BS_CUDA(cudaMemcpyAsync(s->ctl_host->energies, s->p.ctl->energies, sizeof(double) * BS_NUM_ENERGIES,
-                            cudaMemcpyDeviceToHost, s->stream));
-    BS_CUDA(cudaStreamSynchronize(s->stream));
+    // the energies change only in kernels: if none was launched since the last full read of the
+    // control block (which waited for all enqueued work), its copy is current
+    if (s->ctl_read_at != s->launches)
+    {
+        BS_CUDA(cudaMemcpyAsync(s->ctl_host->energies, s->p.ctl->energies, sizeof(double) * BS_NUM_ENERGIES,
+                                cudaMemcpyDeviceToHost, s->stream));
+        BS_CUDA(cudaStreamSynchronize(s->stream));
+    }
     for (int k = 0; k < BS_NUM_ENERGIES; ++k)
         out[k] = s->ctl_host->energies[k];
     return BS_OK;
@@ -1711,6 +1714,7 @@ int bs_batch_autotune(bs_sim *s, int32_t shape[3])
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(s->stream);
     save.free_all();
+    s->ctl_read_at = -1; // the trial runs were not counted as launches
     if (e != cudaSuccess)
         return cuda_fail(s, e, "bs_batch_autotune: trial run");
     s->shape = best;
@@ -1896,11 +1900,11 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
         return fail(s, BS_E_ARG, "bs_adjoint: only the linear steric mode is differentiated");
     if (s->p.nbody > 0 || s->p.probe_on)
         return fail(s, BS_E_ARG, "bs_adjoint: rigid bodies and the probe are not differentiated");
-    if (s->ext_dirty)
-        return fail(s, BS_E_STATE, "bs_adjoint: an external force is pending; step or clear it first");
-    int rc = bs_synchronize(s);
+    int rc = bs_synchronize(s); // ends with a fresh read of the control block
     if (rc)
         return rc;
+    if (s->ctl_host->ext_pending)
+        return fail(s, BS_E_STATE, "bs_adjoint: an external force is pending; step or clear it first");
     Params &p = s->p;
     const int K = std::min(checkpoint, nsteps);
     const int S = (nsteps + K - 1) / K;

@@ -155,7 +155,7 @@ struct Params
     int *inv;                 // caller id -> sorted slot (current layout)
     float4 *pos_build;        // positions at the last pair-list build (sorted)
     // per-particle data in caller order
-    float4 *ext;              // external force for the next step
+    float *ext;               // external force for the next step, float[3n] by caller id
     float4 *force_out;        // forces of a force-only evaluation
     // springs: caller-order CSR (static topology), partner | kEntryStatic | kEntryInactive
     const int *sp_row;        // [n+1]

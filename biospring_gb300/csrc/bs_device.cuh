@@ -702,13 +702,17 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             // ---- external force (SpringNetwork::setForce, SpringNetwork.cpp:438-442) ----
             if (ext_on)
             {
-                const int id = p.perm[lb][s];
-                const float4 xf = p.ext[id];
-                fx += xf.x;
-                fy += xf.y;
-                fz += xf.z;
-                if (MODE == MODE_STEP && (xf.x != 0.f || xf.y != 0.f || xf.z != 0.f))
-                    p.ext[id] = make_float4(0.f, 0.f, 0.f, 0.f);
+                float *xf = p.ext + 3 * static_cast<size_t>(p.perm[lb][s]);
+                const float ex = xf[0], ey = xf[1], ez = xf[2];
+                fx += ex;
+                fy += ey;
+                fz += ez;
+                if (MODE == MODE_STEP && (ex != 0.f || ey != 0.f || ez != 0.f))
+                {
+                    xf[0] = 0.f;
+                    xf[1] = 0.f;
+                    xf[2] = 0.f;
+                }
             }
             // ---- probe (SpringNetwork.cpp:156-182), after every other term ----
             if (p.probe_on)

@@ -991,6 +991,21 @@ static void launch_step_lanes(const Params &p, cudaStream_t st)
     }
 }
 
+// Adds one particle's external force for the next step and marks it pending (bs_set_force).
+__global__ void k_ext_add(Params p, long long i, float fx, float fy, float fz)
+{
+    p.ext[3 * i] += fx;
+    p.ext[3 * i + 1] += fy;
+    p.ext[3 * i + 2] += fz;
+    p.ctl->ext_pending = 1;
+}
+
+int launch_ext_add(const Params &p, long long i, float fx, float fy, float fz, cudaStream_t st)
+{
+    k_ext_add<<<1, 1, 0, st>>>(p, i, fx, fy, fz);
+    return 1;
+}
+
 int launch_step(const Params &p, int mode, cudaStream_t st)
 {
     int launched = launch_step_only(p, mode, st);

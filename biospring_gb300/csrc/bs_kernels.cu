@@ -275,8 +275,11 @@ __global__ void __launch_bounds__(kBuildBlock) k_cell_place(Params p)
     p.tmp_perm[slot] = p.perm[ctl->lbuf][i];
 }
 
-// One warp per cell: orders the cell's particles by caller id (the reference appends them to
-// a cell in index order, nsearch.hpp:376-389), which makes the layout deterministic.
+// One warp per cell: orders the cell's particles by x coordinate, ties by caller id, which makes
+// the layout deterministic and every x-run of cells one x-sorted sequence (the pair-list build
+// bounds its candidates in a run by binary search). Cells are filled in any order by
+// k_cell_place; the reference appends to a cell in index order (nsearch.hpp:376-389), an order
+// no result here depends on.
 __global__ void __launch_bounds__(kBuildBlock) k_cell_sort(Params p)
 {
     Ctl *ctl = p.ctl;
@@ -287,6 +290,10 @@ __global__ void __launch_bounds__(kBuildBlock) k_cell_sort(Params p)
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     int *out = p.perm[ctl->lbuf ^ 1];
+    const float4 *pos = p.pos[ctl->sbuf];
+    auto key_of = [&](int id) -> unsigned long long {
+        return (static_cast<unsigned long long>(f2ord(pos[p.inv[id]].x)) << 32) | static_cast<unsigned int>(id);
+    };
     for (int c = warp; c < nc; c += nwarps)
     {
         const int s0 = p.cell_start[c], s1 = p.cell_start[c + 1];
@@ -294,9 +301,10 @@ __global__ void __launch_bounds__(kBuildBlock) k_cell_sort(Params p)
         for (int e = lane; e < len; e += 32)
         {
             const int id = p.tmp_perm[s0 + e];
+            const unsigned long long key = key_of(id);
             int rank = 0;
             for (int f = 0; f < len; ++f)
-                rank += p.tmp_perm[s0 + f] < id;
+                rank += key_of(p.tmp_perm[s0 + f]) < key;
             out[s0 + rank] = id;
             p.cell_of[s0 + rank] = c;
         }
@@ -343,24 +351,28 @@ __global__ void __launch_bounds__(kBuildBlock) k_reorder(Params p)
     }
 }
 
-// Springs of every slot in the new layout, partners as slots (ELL, column-major).
+// Springs of every slot in the new layout, partners as slots (ELL, column-major). kBuildLanes
+// consecutive threads share a slot and take every kBuildLanes-th spring of its caller-order row,
+// so the row is read with contiguous loads and the partner lookups of a slot overlap.
 __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
 {
     Ctl *ctl = p.ctl;
     if (status_of(ctl) & kRebuildBlocking)
         return;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long g = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int s = static_cast<int>(g / kBuildLanes), t = static_cast<int>(g % kBuildLanes);
     if (s >= p.npad)
         return;
     if (s >= p.n)
     {
-        p.se_deg[s] = 0;
+        if (t == 0)
+            p.se_deg[s] = 0;
         return;
     }
     const int id = p.perm[ctl->lbuf][s];
     const int r0 = p.sp_row[id], r1 = p.sp_row[id + 1];
     const size_t stride = static_cast<size_t>(p.npad);
-    for (int e = r0; e < r1; ++e)
+    for (int e = r0 + t; e < r1; e += kBuildLanes)
     {
         const unsigned int c = p.sp_col[e];
         const unsigned int slot = static_cast<unsigned int>(p.inv[c & kSlotMask]);
@@ -371,7 +383,8 @@ __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
         if (p.se_sid)
             p.se_sid[dst] = p.sp_sid[e];
     }
-    p.se_deg[s] = r1 - r0;
+    if (t == 0)
+        p.se_deg[s] = r1 - r0;
 }
 
 // Typed pair lists from the cell grid: steric (every pair within its cutoff + skin, dynamic and
@@ -381,14 +394,16 @@ __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
 // A block owns one cell and its kPlWarps warps share the cell's home particles (warp w takes
 // every kPlWarps-th one). The grid edge is (cutoff + skin) / kGridDiv, so the neighbourhood is a
 // (2 kGridDiv + 1)^3 block of cells, i.e. (2 kGridDiv + 1)^2 contiguous x-runs of slots, staged
-// in shared memory. For one home particle at a time a warp walks the runs, 32 candidates per pass, one per lane
-// (coalesced loads; the block's warps read the same runs, so they mostly hit L1). Accepted
-// candidates are found with one ballot and appended to the home particle's row-major row at
-// consecutive positions (coalesced stores); the home particle's state stays in registers and
-// lanes never diverge. Rows come out in ascending slot order. Bonded partners are excluded with
-// the home particle's spring partners, sorted in shared memory, of which only those inside the
-// current 32-slot window are compared. In 16-bit mode the steric row holds partner-minus-slot
-// offsets.
+// in shared memory. Cells are x-sorted, so each run is one x-sorted sequence: for one home
+// particle at a time, lane r bounds run r by binary search to the x-interval the list radius
+// allows at that run's y/z distance, and the warp walks the bounded runs, 32 candidates per
+// pass, one per lane. Accepted candidates are found with one ballot and appended to the home
+// particle's row-major row at consecutive positions (coalesced stores); the home particle's
+// state stays in registers and lanes never diverge. Rows come out in ascending slot order.
+// Bonded partners are excluded with the home particle's spring partners, sorted in shared
+// memory, which each lane walks with its own pointer (its candidates ascend). A cell whose
+// neighbourhood exceeds the stage reads whole runs from global memory. In 16-bit mode the
+// steric row holds partner-minus-slot offsets.
 template <bool PL16>
 __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
 {
@@ -399,7 +414,7 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
     __shared__ float4 sh_pos[kPlStage];
     __shared__ int sh_slot[kPlStage];
     __shared__ unsigned char sh_flag[kPlStage];
-    __shared__ int blocked, staged, staged_tot;
+    __shared__ int blocked, staged;
     Ctl *ctl = p.ctl;
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nx = ctl->gnx, ny = ctl->gny, nz = ctl->gnz;
@@ -444,7 +459,6 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
             }
         }
         staged = tot <= kPlStage;
-        staged_tot = tot;
         // every candidate offset of this cell fits 16 bits, or the list goes 32-bit
         if (PL16 && (hi - 1 - h0 > 32767 || lo - (h1 - 1) < -32768))
             atomicOr(&ctl->status, ST_WIDE);
@@ -467,6 +481,9 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
     const float4 *__restrict__ pos = p.pos[sb];
     const unsigned int *__restrict__ fl = p.flags[lb];
     const float r2_0 = p.pl[0].r2, r2_1 = p.pl[1].r2, r2_2 = p.pl[2].r2;
+    const float edge = ctl->gradius;
+    const float gy = static_cast<float>(ctl->gmin[1]), gz = static_cast<float>(ctl->gmin[2]);
+    constexpr float kRowMargin = 1e-2f; // A: covers the FP32 rounding of the cell bounds
     const bool l0 = p.pl[0].on, l1 = p.pl[1].on, l2 = p.pl[2].on, l3 = p.pl[3].on;
     const int cap0 = p.pl[0].cap, cap1 = p.pl[1].cap, cap2 = p.pl[2].cap, cap3 = p.pl[3].cap;
     const size_t stride = static_cast<size_t>(p.npad);
@@ -582,14 +599,63 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
             };
             if (staged)
             {
-                // the staged runs are one ascending sequence of slots: full windows across runs
-                const int tot = staged_tot;
-                for (int jb = 0; jb < tot; jb += 32)
+                // Each run is x-sorted: lane r bounds run r to the candidates whose x lies within
+                // the list radius of the home particle, given the run's distance in y and z
+                // (cell bounds widened by kRowMargin, the grid's outer cells unbounded), by binary
+                // search. Every candidate inside the bounds is still tested exactly; those outside
+                // are farther than the radius. The warp then walks the bounded runs in order.
+                int lo_r = 0, cnt_r = 0;
+                if (lane < kRuns)
                 {
-                    const int q = jb + lane;
-                    const bool jv = q < tot;
-                    const int qc = jv ? q : tot - 1;
-                    window(sh_slot[qc], jv, sh_pos[qc], sh_flag[qc]);
+                    const int j0 = sh_run[lane][0], len = sh_run[lane][1] - j0, o = sh_run[lane][2];
+                    if (len > 0)
+                    {
+                        const int ry = cy + lane % (2 * kGridDiv + 1) - kGridDiv;
+                        const int rz = cz + lane / (2 * kGridDiv + 1) - kGridDiv;
+                        const float y0 = ry == 0 ? -FLT_MAX : gy + ry * edge - kRowMargin;
+                        const float y1 = ry == ny - 1 ? FLT_MAX : gy + (ry + 1) * edge + kRowMargin;
+                        const float z0 = rz == 0 ? -FLT_MAX : gz + rz * edge - kRowMargin;
+                        const float z1 = rz == nz - 1 ? FLT_MAX : gz + (rz + 1) * edge + kRowMargin;
+                        const float dy = fmaxf(0.0f, fmaxf(y0 - pi.y, pi.y - y1));
+                        const float dz = fmaxf(0.0f, fmaxf(z0 - pi.z, pi.z - z1));
+                        const float d2 = dy * dy + dz * dz;
+                        if (d2 < r2max)
+                        {
+                            const float hx = sqrtf(r2max - d2) * 1.0001f + kRowMargin;
+                            const float xa = pi.x - hx, xb = pi.x + hx;
+                            int a = 0, b = len;
+                            while (a < b)
+                            {
+                                const int m = (a + b) >> 1;
+                                if (sh_pos[o + m].x < xa)
+                                    a = m + 1;
+                                else
+                                    b = m;
+                            }
+                            int u = a, v = len;
+                            while (u < v)
+                            {
+                                const int m = (u + v) >> 1;
+                                if (sh_pos[o + m].x <= xb)
+                                    u = m + 1;
+                                else
+                                    v = m;
+                            }
+                            lo_r = o + a;
+                            cnt_r = u - a;
+                        }
+                    }
+                }
+                for (int r = 0; r < kRuns; ++r)
+                {
+                    const int lo = __shfl_sync(0xffffffffu, lo_r, r);
+                    const int cn = __shfl_sync(0xffffffffu, cnt_r, r);
+                    for (int jb = 0; jb < cn; jb += 32)
+                    {
+                        const bool jv = jb + lane < cn;
+                        const int qc = lo + (jv ? jb + lane : cn - 1);
+                        window(sh_slot[qc], jv, sh_pos[qc], sh_flag[qc]);
+                    }
                 }
             }
             else
@@ -936,7 +1002,6 @@ __global__ void __launch_bounds__(kStepBlock) k_diag_pairs(Params p, int term, l
 int launch_rebuild(const Params &p, cudaStream_t st)
 {
     const int nb = (p.n + kBuildBlock - 1) / kBuildBlock;
-    const int nbp = (p.npad + kBuildBlock - 1) / kBuildBlock;
     int bb = (p.n + kBboxBlock - 1) / kBboxBlock;
     bb = bb > 304 ? 304 : (bb < 1 ? 1 : bb);
     int launched = 0;
@@ -955,7 +1020,8 @@ int launch_rebuild(const Params &p, cudaStream_t st)
     k_cell_place<<<nb, kBuildBlock, 0, st>>>(p);
     k_cell_sort<<<1216, kBuildBlock, 0, st>>>(p);
     k_reorder<<<nb, kBuildBlock, 0, st>>>(p);
-    k_spring_ell<<<nbp, kBuildBlock, 0, st>>>(p);
+    k_spring_ell<<<static_cast<int>((static_cast<long long>(p.npad) * kBuildLanes + kBuildBlock - 1) / kBuildBlock),
+                   kBuildBlock, 0, st>>>(p);
     launched += 4;
     if (p.nsys > 0 || p.pl_sparse)
         return launched + launch_batch_pairlist(p, st);

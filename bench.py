@@ -51,6 +51,9 @@ STEP_BYTES_PER_PARTICLE_BASE = 84.0   # positions r+w 32, velocities r+w 32, par
 SPRING_BYTES_PER_ENTRY = 12.0         # partner index + stiffness + rest length
 REBUILD_BYTES_PER_PARTICLE = 104.0    # key 4 + permutation 4 + gather/scatter of x, v, parameters 3 x 32
 CTL_BYTES = 288                       # device control block (status, step count, energies) read per bs_step
+# DRAM bytes (read + write) of one k_step launch on this workload after an L2 flush, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum; profiles/k_step_uniform_lj_100k.md)
+STEP_KERNEL_TRAFFIC_BYTES = 77.43e6 + 2.13e6
 
 
 def peaks() -> dict:
@@ -276,7 +279,9 @@ def run_native(args) -> dict:
             "peak": pk["hbm_gbs"],
             "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"],
-            "traffic": None,
+            "traffic": STEP_KERNEL_TRAFFIC_BYTES,
+            "traffic_src": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
+                           "profiles/k_step_uniform_lj_100k.md",
             "peak_src": pk["src"],
             "algorithmic_bytes_per_launch": alg["step_kernel_bytes"],
             "kernel_ms": kernel_s * 1e3,

@@ -36,6 +36,9 @@ STERIC_MODES = {
 BS_DIELECTRIC_CONSTANT = 0
 BS_DIELECTRIC_DISTANCE = 1
 
+BS_GRID_POTENTIAL = 0
+BS_GRID_DENSITY = 1
+
 BS_TERM_STERIC = 0
 BS_TERM_COULOMB = 1
 BS_TERM_HYDROPHOBIC = 2
@@ -84,6 +87,12 @@ class BsConfig(C.Structure):
         ("probe_epsilon", C.c_double),
         ("probe_radius", C.c_double),
         ("probe_charge", C.c_double),
+        ("potentialgrid_enable", C.c_int32),
+        ("densitygrid_enable", C.c_int32),
+        ("potentialgrid_scale", C.c_double),
+        ("densitygrid_scale", C.c_double),
+        ("potentialgrid_path", C.c_char * 512),
+        ("densitygrid_path", C.c_char * 512),
     ]
 
     def to_dict(self) -> dict:
@@ -106,6 +115,10 @@ SIGNATURES = {
                                       _f32p, _f32p, _u8p]),
     "bs_upload_springs": (C.c_int, [C.c_void_p, C.c_int64, _i32p, _f32p, _f32p]),
     "bs_set_rigid_bodies": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _i32p]),
+    "bs_set_field_grid": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _f64p, _f64p, _f32p]),
+    "bs_read_dx": (C.c_int, [C.c_char_p, _i32p, _f64p, _f64p, _f32p, C.c_char_p, C.c_size_t]),
+    "bs_get_field_grid": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _f32p]),
+    "bs_set_burying": (C.c_int, [C.c_void_p, _f32p]),
     "bs_setup": (C.c_int, [C.c_void_p, C.POINTER(BsConfig)]),
     "bs_step": (C.c_int, [C.c_void_p, C.c_int32]),
     "bs_step_async": (C.c_int, [C.c_void_p, C.c_int32]),

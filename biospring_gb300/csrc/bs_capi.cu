@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/biospring_gb300.h"
+#include "bs_field.h"
 #include "bs_kernels.cuh"
 
 using namespace bsg;
@@ -56,6 +57,16 @@ struct bs_sim
     std::vector<float> sp_r0, sp_k;
     std::unordered_set<uint64_t> sp_seen;
     std::vector<std::vector<int32_t>> bodies;
+    // field grids given with bs_set_field_grid (else read from the configured path at set-up)
+    struct FieldHost
+    {
+        bool set = false;
+        int shape[3] = {0, 0, 0};
+        double origin[3] = {0.0, 0.0, 0.0}, spacing[3] = {1.0, 1.0, 1.0};
+        std::vector<float> scalar;
+        std::vector<float> cells; // 4 per cell after set-up: scalar, force vector
+    } field[2];
+    std::vector<float> burying; // caller order; empty: 1 for every particle
     bs_config cfg{};
     bool have_cfg = false;
     bool ready = false;
@@ -508,6 +519,8 @@ int bs_default_config(bs_config *c)
     c->probe_epsilon = 1.0;
     c->probe_radius = 1.0;
     c->probe_charge = 0.0;
+    c->potentialgrid_scale = 1.0;
+    c->densitygrid_scale = 1.0;
     return BS_OK;
 }
 
@@ -633,6 +646,72 @@ int bs_set_rigid_bodies(bs_sim *s, int32_t nb, const int32_t *offsets, const int
     }
     s->bodies = bodies;
     s->ready = false;
+    return BS_OK;
+}
+
+int bs_set_field_grid(bs_sim *s, int32_t which, const int32_t shape[3], const double origin[3],
+                      const double spacing[3], const float *scalar)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if ((which != BS_GRID_POTENTIAL && which != BS_GRID_DENSITY) || !shape || !origin || !spacing || !scalar)
+        return fail(s, BS_E_ARG, "bs_set_field_grid: bad arguments");
+    size_t cells = 1;
+    for (int a = 0; a < 3; ++a)
+    {
+        if (shape[a] < 1 || !(spacing[a] > 0.0) || !std::isfinite(spacing[a]) || !std::isfinite(origin[a]))
+            return fail(s, BS_E_ARG, "bs_set_field_grid: shape >= 1, spacing > 0 and a finite origin are required");
+        cells *= static_cast<size_t>(shape[a]);
+    }
+    // the reference re-derives the shape from the box (GridCoordinatesSystem.hpp:180-191)
+    const long counts[3] = {shape[0], shape[1], shape[2]};
+    int derived[3];
+    bsg::field_shape(counts, origin, spacing, derived);
+    if (derived[0] != shape[0] || derived[1] != shape[1] || derived[2] != shape[2])
+        return fail(s, BS_E_ARG, "bs_set_field_grid: the box origin + shape * spacing rounds to another shape");
+    auto &f = s->field[which];
+    f.set = true;
+    for (int a = 0; a < 3; ++a)
+    {
+        f.shape[a] = shape[a];
+        f.origin[a] = origin[a];
+        f.spacing[a] = spacing[a];
+    }
+    f.scalar.assign(scalar, scalar + cells);
+    s->ready = false;
+    return BS_OK;
+}
+
+int bs_get_field_grid(bs_sim *s, int32_t which, int32_t shape[3], float *out)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if ((which != BS_GRID_POTENTIAL && which != BS_GRID_DENSITY) || !shape)
+        return fail(s, BS_E_ARG, "bs_get_field_grid: bad arguments");
+    if (!s->ready || s->field[which].cells.empty())
+        return fail(s, BS_E_STATE, "bs_get_field_grid: no such grid in the current set-up");
+    for (int a = 0; a < 3; ++a)
+        shape[a] = s->field[which].shape[a];
+    if (out)
+        std::memcpy(out, s->field[which].cells.data(), sizeof(float) * s->field[which].cells.size());
+    return BS_OK;
+}
+
+int bs_set_burying(bs_sim *s, const float *burying)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!burying)
+        return fail(s, BS_E_ARG, "bs_set_burying: null argument");
+    s->burying.assign(burying, burying + s->n);
+    if (s->ready && s->p.bur[0])
+    {
+        // into the current layout, in stream order
+        BS_CUDA(cudaStreamSynchronize(s->stream));
+        BS_CUDA(cudaMemcpyAsync(s->staging, burying, sizeof(float) * s->n, cudaMemcpyHostToDevice, s->stream));
+        s->launches += launch_set_burying(s->p, s->staging, s->stream);
+        BS_CUDA(cudaStreamSynchronize(s->stream));
+    }
     return BS_OK;
 }
 
@@ -833,7 +912,7 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     for (int t = 0; t < kLists; ++t)
         BS_CUDA(s->dev.alloc(&p.pl[t].cnt, npad));
     BS_CUDA(s->dev.alloc(&p.cell_of, npad));
-    BS_CUDA(s->dev.alloc(&p.tmp_perm, npad));
+    BS_CUDA(s->dev.alloc(&p.tmp_key, npad));
     s->step_blocks = static_cast<int>((static_cast<long long>(p.n) * 8 + kStepBlock - 1) / kStepBlock);
     p.blk_cap = s->step_blocks;
     BS_CUDA(s->dev.alloc(&p.blk_energy, energy_scratch_doubles(s->step_blocks)));
@@ -955,6 +1034,69 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     BS_CUDA(cudaMemcpyAsync(d_r0, rr.data(), sizeof(float) * std::max(nnz, 1), cudaMemcpyHostToDevice, s->stream));
     BS_CUDA(cudaMemsetAsync(p.ext, 0, sizeof(float) * 3 * n, s->stream));
     BS_CUDA(cudaMemsetAsync(p.force_out, 0, sizeof(float4) * n, s->stream));
+    // ---- field grids (SpringNetwork::_setupElectrostatic / _setupDensityGrid,
+    // SpringNetwork.cpp:712-747): the potential map acts when coulomb.enable is set too ----
+    for (int g = 0; g < 2; ++g)
+    {
+        auto &f = s->field[g];
+        f.cells.clear();
+        const bool on = g == 0 ? (c.potentialgrid_enable && c.coulomb_enable) : c.densitygrid_enable != 0;
+        if (!on)
+            continue;
+        if (!f.set)
+        {
+            const char *path = g == 0 ? c.potentialgrid_path : c.densitygrid_path;
+            std::string msg;
+            std::vector<float> v;
+            int sh[3];
+            if (!path[0])
+                return fail(s, BS_E_ARG, std::string(g == 0 ? "potentialgrid" : "densitygrid") +
+                                             ".enable: no grid (give a path or call bs_set_field_grid)");
+            if (!bsg::read_dx(path, sh, f.origin, f.spacing, &v, msg))
+                return fail(s, BS_E_ARG, msg);
+            for (int a = 0; a < 3; ++a)
+                f.shape[a] = sh[a];
+            f.scalar = v;
+        }
+        const size_t ncell = f.scalar.size();
+        f.cells.resize(4 * ncell);
+        bsg::field_cells(f.shape, f.spacing, f.scalar.data(), f.cells.data());
+        float4 *d = nullptr;
+        BS_CUDA(s->dev.alloc(&d, std::max<size_t>(ncell, 1)));
+        BS_CUDA(cudaMemcpyAsync(d, f.cells.data(), sizeof(float) * 4 * ncell, cudaMemcpyHostToDevice, s->stream));
+        p.fgrid[g] = d;
+        p.fg_on[g] = 1;
+        p.fg_scale[g] = static_cast<float>(g == 0 ? c.potentialgrid_scale : c.densitygrid_scale);
+        for (int a = 0; a < 3; ++a)
+        {
+            p.fg_n[g][a] = f.shape[a];
+            p.fg_o[g][a] = f.origin[a];
+            p.fg_h[g][a] = f.spacing[a];
+            p.fg_of[g][a] = static_cast<float>(f.origin[a]);
+            p.fg_ih[g][a] = static_cast<float>(1.0 / f.spacing[a]);
+            // in-grid test min <= x <= max - 1e-6 in double (GridCoordinatesSystem.hpp:206-218), for a
+            // float x: the smallest float >= min and the largest float <= max - 1e-6
+            const double lo = f.origin[a];
+            const double hi = (f.origin[a] + static_cast<double>(f.shape[a]) * f.spacing[a]) - 1e-6;
+            float flo = static_cast<float>(lo), fhi = static_cast<float>(hi);
+            if (static_cast<double>(flo) < lo)
+                flo = std::nextafter(flo, INFINITY);
+            if (static_cast<double>(fhi) > hi)
+                fhi = std::nextafter(fhi, -INFINITY);
+            p.fg_lo[g][a] = flo;
+            p.fg_hi[g][a] = fhi;
+        }
+        if (g == 1)
+        {
+            std::vector<float> b0(npad, 1.0f);
+            if (!s->burying.empty())
+                std::copy(s->burying.begin(), s->burying.end(), b0.begin());
+            for (int b = 0; b < 2; ++b)
+                BS_CUDA(s->dev.alloc(&p.bur[b], npad));
+            BS_CUDA(cudaMemcpyAsync(p.bur[0], b0.data(), sizeof(float) * npad, cudaMemcpyHostToDevice, s->stream));
+            BS_CUDA(cudaStreamSynchronize(s->stream)); // b0 is a local
+        }
+    }
     std::memset(s->ctl_host, 0, sizeof(Ctl));
     for (int k = 0; k < 3; ++k)
     {
@@ -1900,6 +2042,8 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
         return fail(s, BS_E_ARG, "bs_adjoint: only the linear steric mode is differentiated");
     if (s->p.nbody > 0 || s->p.probe_on)
         return fail(s, BS_E_ARG, "bs_adjoint: rigid bodies and the probe are not differentiated");
+    if (s->p.fg_on[0] || s->p.fg_on[1])
+        return fail(s, BS_E_ARG, "bs_adjoint: field-grid forces are not differentiated");
     int rc = bs_synchronize(s); // ends with a fresh read of the control block
     if (rc)
         return rc;

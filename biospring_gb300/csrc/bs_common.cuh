@@ -179,7 +179,7 @@ struct Params
     int *cell_cnt;            // [cell_cap + 1]
     int *cell_start;          // [cell_cap + 1]
     int *cell_fill;           // [cell_cap]
-    int *tmp_perm;            // [npad]
+    unsigned long long *tmp_key; // [npad] cell-sort key of each placed particle (x bits, caller id)
     int cell_cap;
     int *tile_sum;            // [cell_cap / kScanTile + 2] per-tile totals of the cell scan
     int pl_sparse;            // build the pair lists one warp per particle (few particles per cell)
@@ -233,6 +233,17 @@ struct Params
     int probe_on, probe_steric, probe_elec;
     float probe_P, probe_F, probe_q, probe_mass;
     float4 *probe_f;          // [npad]
+    // field grids, 0 = electrostatic potential (on charges), 1 = density (on burying); cells in
+    // OpenDX order (scalar, force vector). A float x lies in the grid along an axis iff
+    // fg_lo <= x <= fg_hi, the float translation of the reference's double bounds test.
+    const float4 *fgrid[2];
+    int fg_on[2];
+    int fg_n[2][3];
+    double fg_o[2][3], fg_h[2][3];  // origin and cell size, as the reference holds them
+    float fg_lo[2][3], fg_hi[2][3];
+    float fg_of[2][3], fg_ih[2][3]; // origin and 1 / cell size in float, for the fast cell index
+    float fg_scale[2];              // potentialgrid.scale (force and energy), densitygrid.scale
+    float *bur[2];                  // per-particle burying, layout lb
 };
 
 constexpr int kMaxCluster = 16;

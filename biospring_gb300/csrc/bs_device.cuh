@@ -558,6 +558,69 @@ __device__ __forceinline__ void probe_pair(const Params &p, const float4 &prb, f
     }
 }
 
+// Cell of field grid g holding the particle at pi, or -1 when the particle is outside the grid's
+// box (GridCoordinatesSystem::is_out_of_grid, GridCoordinatesSystem.hpp:206-218). The index along
+// an axis is trunc((x - origin) / cell size) evaluated in double (GridCoordinatesSystem.hpp:85-94);
+// the float estimate decides unless it lies within its error bound of an integer, where the
+// double expression is evaluated.
+__device__ __forceinline__ int field_cell(const Params &p, int g, const float4 &pi)
+{
+    const float x[3] = {pi.x, pi.y, pi.z};
+    int idx[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+    {
+        if (!(x[a] >= p.fg_lo[g][a] && x[a] <= p.fg_hi[g][a]))
+            return -1;
+        const float t = (x[a] - p.fg_of[g][a]) * p.fg_ih[g][a];
+        int c;
+        if (fabsf(t - rintf(t)) < 1e-3f + 4e-7f * fabsf(t))
+            c = static_cast<int>(__ddiv_rn(__dsub_rn(static_cast<double>(x[a]), p.fg_o[g][a]), p.fg_h[g][a]));
+        else
+            c = static_cast<int>(t);
+        idx[a] = min(max(c, 0), p.fg_n[g][a] - 1);
+    }
+    return (idx[0] * p.fg_n[g][1] + idx[1]) * p.fg_n[g][2] + idx[2];
+}
+
+// Field-grid forces of one dynamic particle (SpringNetwork.cpp:110-118): the potential map's
+// force q v s and energy s * field_energy(scalar, q) (Particle.cpp:161-189,
+// electrostatic_field.hpp:16-23), and the density map's force b v s' (Particle.cpp:136-159),
+// with the reference's float products and double unit steps.
+__device__ __forceinline__ void field_forces(const Params &p, const float4 &pi, float q, float bur, float &fx,
+                                             float &fy, float &fz, float &e_elec)
+{
+    if (p.fg_on[0])
+    {
+        const int c = field_cell(p, 0, pi);
+        if (c >= 0)
+        {
+            const float4 v = p.fgrid[0][c];
+            const float gs = p.fg_scale[0];
+            fx += __fmul_rn(__fmul_rn(v.y, q), gs);
+            fy += __fmul_rn(__fmul_rn(v.z, q), gs);
+            fz += __fmul_rn(__fmul_rn(v.w, q), gs);
+            float en = __fmul_rn(v.x, q);
+            en = __double2float_rn(__dmul_rn(static_cast<double>(en), 1.3806504E-23));
+            en = __double2float_rn(__dmul_rn(static_cast<double>(en), 1.0E-3));
+            en = __double2float_rn(__dmul_rn(static_cast<double>(en), 6.02214169E23));
+            e_elec += __fmul_rn(gs, en);
+        }
+    }
+    if (p.fg_on[1])
+    {
+        const int c = field_cell(p, 1, pi);
+        if (c >= 0)
+        {
+            const float4 v = p.fgrid[1][c];
+            const float gs = p.fg_scale[1];
+            fx += __fmul_rn(__fmul_rn(v.y, bur), gs);
+            fy += __fmul_rn(__fmul_rn(v.z, bur), gs);
+            fz += __fmul_rn(__fmul_rn(v.w, bur), gs);
+        }
+    }
+}
+
 // Sum over the T consecutive lanes of a particle group (result in every lane of the group).
 template <int T> __device__ __forceinline__ float group_sum(float v)
 {
@@ -676,6 +739,9 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
         else
         {
             const float4 v = p.vel[sb][s];
+            // ---- field grids (SpringNetwork.cpp:110-118) ----
+            if (p.fg_on[0] || p.fg_on[1])
+                field_forces(p, pi, p.chg[lb][s], p.fg_on[1] ? p.bur[lb][s] : 0.0f, fx, fy, fz, e[2]);
             // ---- viscosity (Particle.cpp:80-84) ----
             if (p.visc_on)
             {

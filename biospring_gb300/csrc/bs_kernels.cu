@@ -272,7 +272,10 @@ __global__ void __launch_bounds__(kBuildBlock) k_cell_place(Params p)
     if (i >= p.n)
         return;
     const int slot = atomicAdd(&p.cell_fill[p.cell_of[i]], 1);
-    p.tmp_perm[slot] = p.perm[ctl->lbuf][i];
+    const int id = p.perm[ctl->lbuf][i];
+    // the order key of k_cell_sort: x coordinate, then caller id
+    p.tmp_key[slot] = (static_cast<unsigned long long>(f2ord(p.pos[ctl->sbuf][i].x)) << 32) |
+                      static_cast<unsigned int>(id);
 }
 
 // One warp per cell: orders the cell's particles by x coordinate, ties by caller id, which makes
@@ -290,22 +293,18 @@ __global__ void __launch_bounds__(kBuildBlock) k_cell_sort(Params p)
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     int *out = p.perm[ctl->lbuf ^ 1];
-    const float4 *pos = p.pos[ctl->sbuf];
-    auto key_of = [&](int id) -> unsigned long long {
-        return (static_cast<unsigned long long>(f2ord(pos[p.inv[id]].x)) << 32) | static_cast<unsigned int>(id);
-    };
+    const unsigned long long *__restrict__ key = p.tmp_key;
     for (int c = warp; c < nc; c += nwarps)
     {
         const int s0 = p.cell_start[c], s1 = p.cell_start[c + 1];
         const int len = s1 - s0;
         for (int e = lane; e < len; e += 32)
         {
-            const int id = p.tmp_perm[s0 + e];
-            const unsigned long long key = key_of(id);
+            const unsigned long long ke = key[s0 + e];
             int rank = 0;
             for (int f = 0; f < len; ++f)
-                rank += key_of(p.tmp_perm[s0 + f]) < key;
-            out[s0 + rank] = id;
+                rank += key[s0 + f] < ke;
+            out[s0 + rank] = static_cast<int>(ke & 0xffffffffu);
             p.cell_of[s0 + rank] = c;
         }
     }
@@ -332,6 +331,8 @@ __global__ void __launch_bounds__(kBuildBlock) k_reorder(Params p)
         p.fhi[lb ^ 1][i] = p.fhi[lb][old];
         p.chg[lb ^ 1][i] = p.chg[lb][old];
         p.hyd[lb ^ 1][i] = p.hyd[lb][old];
+        if (p.bur[0])
+            p.bur[lb ^ 1][i] = p.bur[lb][old];
         p.flags[lb ^ 1][i] = p.flags[lb][old];
         p.iprm[lb ^ 1][i] = p.iprm[lb][old];
         p.pos_build[i] = q;
@@ -1055,6 +1056,20 @@ static void launch_step_lanes(const Params &p, cudaStream_t st)
         k_step<MODE, SM, 4><<<nb, kStepKernelBlock, 0, st>>>(p);
         break;
     }
+}
+
+// Burying of every particle into the current layout (bs_set_burying), from caller order.
+__global__ void k_set_burying(Params p, const float *b)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id < p.n)
+        p.bur[p.ctl->lbuf][p.inv[id]] = b[id];
+}
+
+int launch_set_burying(const Params &p, const float *b, cudaStream_t st)
+{
+    k_set_burying<<<(p.n + 255) / 256, 256, 0, st>>>(p, b);
+    return 1;
 }
 
 // Adds one particle's external force for the next step and marks it pending (bs_set_force).

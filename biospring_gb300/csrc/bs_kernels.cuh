@@ -53,6 +53,7 @@ int launch_step(const Params &p, int mode, cudaStream_t stream);      // step ke
 int launch_step_only(const Params &p, int mode, cudaStream_t stream); // the step kernel alone
 int launch_rigid(const Params &p, cudaStream_t stream);               // bs_rigid.cu
 int launch_ext_add(const Params &p, long long i, float fx, float fy, float fz, cudaStream_t stream);
+int launch_set_burying(const Params &p, const float *burying, cudaStream_t stream);
 int launch_unsort(const Params &p, int what, float *out3, cudaStream_t stream);
 int launch_diag_cells(const Params &p, float cutoff, float skin, uint32_t need_flag, long long *out,
                       cudaStream_t stream);

@@ -170,6 +170,10 @@ extern "C" int bs_config_parse_msp(const char *text, bs_config *cfg, char *err, 
                 c.probe_electrostatic = b;
             else if (name == "probe.enablesteric")
                 c.probe_steric = b;
+            else if (name == "potentialgrid.enable")
+                c.potentialgrid_enable = b;
+            else if (name == "densitygrid.enable")
+                c.densitygrid_enable = b;
         }
         else if (name == "steric.mode")
         {
@@ -202,6 +206,14 @@ extern "C" int bs_config_parse_msp(const char *text, bs_config *cfg, char *err, 
                 c.nbsteps = v;
             else
                 c.rebuild_every = v;
+        }
+        else if (name == "potentialgrid.path" || name == "densitygrid.path")
+        {
+            char *dst = name[0] == 'p' ? c.potentialgrid_path : c.densitygrid_path;
+            if (value.size() >= sizeof(c.potentialgrid_path))
+                return perr(err, err_len, name + ": path longer than " +
+                                              std::to_string(sizeof(c.potentialgrid_path) - 1) + " characters");
+            std::snprintf(dst, sizeof(c.potentialgrid_path), "%s", value.c_str());
         }
         else if (param == "path" || param == "vector")
         {
@@ -255,6 +267,10 @@ extern "C" int bs_config_parse_msp(const char *text, bs_config *cfg, char *err, 
                 c.probe_radius = d;
             else if (name == "probe.charge")
                 c.probe_charge = d;
+            else if (name == "potentialgrid.scale")
+                c.potentialgrid_scale = d;
+            else if (name == "densitygrid.scale")
+                c.densitygrid_scale = d;
         }
     }
     *cfg = c;

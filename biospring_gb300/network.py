@@ -80,6 +80,31 @@ class SpringNetwork:
         self._check(self._lib.bs_upload_springs(self._h, ij.shape[0], ptr(ij, C.c_int32), ptr(r0, C.c_float),
                                                 ptr(k, C.c_float)), self._h)
 
+    # -- field grids (potentialgrid.*, densitygrid.*) ------------------------------------------
+    def setFieldGrid(self, which: int, scalar, origin, spacing):
+        """Map `which` (capi.BS_GRID_POTENTIAL or BS_GRID_DENSITY) from a (n0, n1, n2) array of
+        scalar values on a grid of cell size `spacing` from `origin`; call before :meth:`setup`."""
+        sc = np.ascontiguousarray(scalar, dtype=np.float32)
+        shape = np.asarray(sc.shape, dtype=np.int32)
+        o = np.ascontiguousarray(origin, dtype=np.float64)
+        h = np.ascontiguousarray(spacing, dtype=np.float64)
+        self._check(self._lib.bs_set_field_grid(self._h, int(which), ptr(shape, C.c_int32), ptr(o, C.c_double),
+                                                ptr(h, C.c_double), ptr(sc, C.c_float)), self._h)
+
+    def fieldGrid(self, which: int) -> np.ndarray:
+        """The map after set-up, (n0, n1, n2, 4): scalar and force vector of every cell."""
+        shape = np.zeros(3, dtype=np.int32)
+        self._check(self._lib.bs_get_field_grid(self._h, int(which), ptr(shape, C.c_int32), None), self._h)
+        out = np.zeros(tuple(int(v) for v in shape) + (4,), dtype=np.float32)
+        self._check(self._lib.bs_get_field_grid(self._h, int(which), ptr(shape, C.c_int32), ptr(out, C.c_float)),
+                    self._h)
+        return out
+
+    def setBurying(self, burying):
+        """Per-particle burying, the weight of the density-map force (default 1)."""
+        b = _f32(burying)
+        self._check(self._lib.bs_set_burying(self._h, ptr(b, C.c_float)), self._h)
+
     def setRigidBodies(self, bodies):
         offsets = np.zeros(len(bodies) + 1, dtype=np.int32)
         for b, ids in enumerate(bodies):

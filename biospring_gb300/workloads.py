@@ -229,3 +229,41 @@ def adjoint_fit(n: int = 10_000, seed: int = 4, amplitude: float = 2.0, nsteps: 
     target = (s.xyz.astype(np.float64) + smooth_displacement(s.xyz, seed + 17, amplitude)).astype(np.float32)
     s.meta["nsteps"] = nsteps
     return s, target, nsteps
+
+
+def field_map(shape, origin, spacing, seed: int, amplitude: float = 100.0, centres: int = 6) -> np.ndarray:
+    """A smooth synthetic scalar map (a sum of Gaussian wells and hills, like an electrostatic
+    potential in kT/e around charged groups) on a regular grid, float32 of the given shape."""
+    rng = np.random.default_rng(seed)
+    axes = [origin[a] + spacing[a] * np.arange(shape[a]) for a in range(3)]
+    gx, gy, gz = np.meshgrid(*axes, indexing="ij")
+    lo = np.array(origin, np.float64)
+    hi = lo + np.array(spacing, np.float64) * np.array(shape)
+    out = np.zeros(tuple(shape), np.float64)
+    for _ in range(centres):
+        c = rng.uniform(lo, hi)
+        w = rng.uniform(0.15, 0.35) * float(np.min(hi - lo))
+        out += rng.choice([-1.0, 1.0]) * amplitude * np.exp(-((gx - c[0]) ** 2 + (gy - c[1]) ** 2 + (gz - c[2]) ** 2)
+                                                             / (2.0 * w * w))
+    return out.astype(np.float32)
+
+
+def write_dx(path: str, scalar: np.ndarray, origin, spacing) -> None:
+    """Writes a scalar map as an OpenDX regular grid (the layout OpenDXReader reads: counts,
+    origin, three delta lines, two object lines, then the values three per line, z fastest).
+    Values are printed with 9 significant digits, so float32 values read back exactly."""
+    sc = np.ascontiguousarray(scalar, np.float32)
+    n0, n1, n2 = sc.shape
+    with open(path, "w") as f:
+        f.write("# synthetic map\n")
+        f.write(f"object 1 class gridpositions counts {n0} {n1} {n2}\n")
+        f.write("origin {:.9g} {:.9g} {:.9g}\n".format(*origin))
+        f.write(f"delta {spacing[0]:.9g} 0 0\ndelta 0 {spacing[1]:.9g} 0\ndelta 0 0 {spacing[2]:.9g}\n")
+        f.write(f"object 2 class gridconnections counts {n0} {n1} {n2}\n")
+        f.write(f'object 3 class array type double rank 0 items {sc.size} data follows\n')
+        flat = sc.reshape(-1)
+        for i in range(0, flat.size, 3):
+            f.write(" ".join(f"{v:.9g}" for v in flat[i:i + 3]) + "\n")
+        f.write('attribute "dep" string "positions"\n')
+        f.write('object "regular positions regular connections" class field\n')
+        f.write('component "positions" value 1\ncomponent "connections" value 2\ncomponent "data" value 3\n')

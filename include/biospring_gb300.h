@@ -112,6 +112,17 @@ typedef struct bs_config {
     int32_t probe_steric;        /* probe.enablesteric */
     double probe_x, probe_y, probe_z;
     double probe_mass, probe_epsilon, probe_radius, probe_charge;
+    /* potentialgrid.* and densitygrid.* (GridSetting, Setting.hpp:192-222): forces read from a
+       scalar map on a regular grid (SpringNetwork.cpp:110-118, Particle.cpp:136-189). The
+       potential map acts on charges when coulomb.enable is set too; the density map acts on
+       every dynamic particle through its burying. A path is read at bs_setup unless a grid was
+       given with bs_set_field_grid. */
+    int32_t potentialgrid_enable;
+    int32_t densitygrid_enable;
+    double potentialgrid_scale;
+    double densitygrid_scale;
+    char potentialgrid_path[512];
+    char densitygrid_path[512];
 } bs_config;
 
 typedef struct bs_sim bs_sim;
@@ -157,6 +168,34 @@ int bs_upload_springs(bs_sim *sim, int64_t s, const int32_t *ij, const float *eq
  * springs whose two ends are rigid stop acting (RigidBody.cpp:41-53).
  * Effective when rigidbody_enable is set. */
 int bs_set_rigid_bodies(bs_sim *sim, int32_t nbodies, const int32_t *offsets, const int32_t *ids);
+
+/* Field grids (PotentialGrid, src/grid/PotentialGrid.hpp): which = BS_GRID_POTENTIAL or
+ * BS_GRID_DENSITY. A grid of shape[0] x shape[1] x shape[2] cells of size spacing (A) from
+ * origin, scalar values in OpenDX order (scalar[(i * shape[1] + j) * shape[2] + k]). The library
+ * derives each cell's force vector as PotentialGrid::compute_gradient does (PotentialGrid.cpp:
+ * 20-59); a particle takes the cell holding it, and one outside the box gets no field force and
+ * no field energy (Particle.cpp:136-189). Replaces reading the map at set-up
+ * (SpringNetwork.cpp:717-747); call before bs_setup. */
+#define BS_GRID_POTENTIAL 0
+#define BS_GRID_DENSITY 1
+int bs_set_field_grid(bs_sim *sim, int32_t which, const int32_t shape[3], const double origin[3],
+                      const double spacing[3], const float *scalar);
+
+/* Reads an OpenDX scalar map as OpenDXReader::read does (src/IO/OpenDXReader.cpp): the grid
+ * shape the reference derives from the file's box, origin and spacing, then the values. With
+ * scalar NULL only the header is read (shape, origin, spacing); otherwise scalar must hold
+ * shape[0] * shape[1] * shape[2] floats. */
+int bs_read_dx(const char *path, int32_t shape[3], double origin[3], double spacing[3], float *scalar,
+               char *err, size_t err_len);
+
+/* The grid after set-up: its shape and, when out is not NULL, 4 floats per cell in OpenDX order:
+ * the scalar and the force vector (PotentialCell, PotentialGrid.hpp:12-16); out holds
+ * 4 * shape[0] * shape[1] * shape[2] floats. */
+int bs_get_field_grid(bs_sim *sim, int32_t which, int32_t shape[3], float *out);
+
+/* Per-particle burying (ParticleProperty::setBurying, ParticleProperty.h:61; default 1), the
+ * weight of the density-grid force, caller order. */
+int bs_set_burying(bs_sim *sim, const float *burying);
 
 /* Validates the configuration, uploads everything and builds the first cell list
  * and pair list (replaces SpringNetwork::setup, SpringNetwork.cpp:646-737).

@@ -60,6 +60,7 @@ const double C_VACUUMPERMITIVITY = 8.854187817E-12;
 const double C_AVOGADRO = 6.02214169E23;
 const double C_COULOMB_K = 1.0 / (4.0 * C_PI * C_VACUUMPERMITIVITY);
 const double C_NEWTON_TO_DAFS2 = C_METER_TO_ANGSTROM * C_KILOGRAM_TO_DALTON * C_FEMTOSECOND_TO_SECOND * C_FEMTOSECOND_TO_SECOND;
+const double C_BOLTZMANN_J_PER_K = 1.3806504E-23;
 const double C_MIN_DIST_ELEC = 0.001;
 const double C_MIN_DIST_VDW = 0.1;
 const double C_KINETIC = (C_ANGSTROM_TO_METER * C_SECOND_TO_FEMTOSECOND) * (C_ANGSTROM_TO_METER * C_SECOND_TO_FEMTOSECOND) *
@@ -471,9 +472,76 @@ inline Q qinverse(Q q)
     return {im.x, im.y, im.z, s};
 }
 
+// A field grid (PotentialGrid, src/grid/PotentialGrid.hpp): scalar and force vector per cell,
+// OpenDX order, over the box [lo, hi] (GridCoordinatesSystem.hpp:154-218).
+struct Field
+{
+    bool on = false;
+    int n[3] = {0, 0, 0};
+    double o[3] = {0, 0, 0}, h[3] = {1, 1, 1}, hi[3] = {0, 0, 0};
+    std::vector<float> sc, gx, gy, gz;
+
+    // PotentialGrid::compute_gradient (PotentialGrid.cpp:20-59)
+    void set(const int32_t shape[3], const double origin[3], const double spacing[3], const float * scalar)
+    {
+        for (int a = 0; a < 3; ++a)
+        {
+            n[a] = shape[a];
+            o[a] = origin[a];
+            h[a] = spacing[a];
+            hi[a] = origin[a] + static_cast<double>(static_cast<size_t>(shape[a])) * spacing[a];
+        }
+        const size_t total = static_cast<size_t>(n[0]) * n[1] * n[2];
+        sc.assign(scalar, scalar + total);
+        gx.assign(total, 0.0f);
+        gy.assign(total, 0.0f);
+        gz.assign(total, 0.0f);
+        const float scale = static_cast<float>(C_BOLTZMANN_J_PER_K * C_METER_TO_ANGSTROM * C_NEWTON_TO_DAFS2);
+        const float dx = static_cast<float>(h[0]), dy = static_cast<float>(h[1]), dz = static_cast<float>(h[2]);
+        auto id = [&](size_t i, size_t j, size_t k) { return (i * n[1] + j) * n[2] + k; };
+        auto grad = [](float cur, float prev, float next, float cs) -> float {
+            return ((cur - prev) + (next - cur)) / (cs * 2.0);
+        };
+        for (size_t i = 0; i < static_cast<size_t>(n[0]); ++i)
+            for (size_t j = 0; j < static_cast<size_t>(n[1]); ++j)
+                for (size_t k = 0; k < static_cast<size_t>(n[2]); ++k)
+                {
+                    const size_t c = id(i, j, k);
+                    V3 g{0.0f, 0.0f, 0.0f};
+                    if (i > 0 && i < static_cast<size_t>(n[0]) - 1)
+                        g.x = grad(sc[c], sc[id(i - 1, j, k)], sc[id(i + 1, j, k)], dx);
+                    if (j > 0 && j < static_cast<size_t>(n[1]) - 1)
+                        g.y = grad(sc[c], sc[id(i, j - 1, k)], sc[id(i, j + 1, k)], dy);
+                    if (k > 0 && k < static_cast<size_t>(n[2]) - 1)
+                        g.z = grad(sc[c], sc[id(i, j, k - 1)], sc[id(i, j, k + 1)], dz);
+                    g = mul(g, -scale);
+                    gx[c] = g.x;
+                    gy[c] = g.y;
+                    gz[c] = g.z;
+                }
+    }
+
+    // the cell holding (x, y, z), or -1 outside the box (is_out_of_grid, then cell_coordinates:
+    // GridCoordinatesSystem.hpp:85-94, 206-218)
+    int64_t cell(float x, float y, float z) const
+    {
+        const double p[3] = {x, y, z};
+        int c[3];
+        for (int a = 0; a < 3; ++a)
+        {
+            if (p[a] < o[a] || p[a] > hi[a] - 1e-6)
+                return -1;
+            c[a] = static_cast<int>((p[a] - o[a]) / h[a]);
+        }
+        return (static_cast<int64_t>(c[0]) * n[1] + c[1]) * n[2] + c[2];
+    }
+};
+
 struct Sim
 {
     bs_config cfg{};
+    Field field[2]; // potential (electrostatic field), density
+    std::vector<float> burying;
     FF ff;
     int64_t n = 0;
     std::vector<float> x, y, z, vx, vy, vz, fx, fy, fz, mass, charge, radius, eps, hydro, sasa, transfer;
@@ -661,6 +729,34 @@ struct Sim
             const int64_t i = dynamic[t];
             if (cfg.coulomb_enable && charged[i] && grid[1].active)
                 pair_term<BS_TERM_COULOMB>(i, d_elec[t]);
+            if (cfg.coulomb_enable && field[0].on)
+            {
+                // Particle::addElectrostaticFieldForce (Particle.cpp:161-189)
+                const int64_t c = field[0].cell(x[i], y[i], z[i]);
+                if (c >= 0)
+                {
+                    const float gs = static_cast<float>(cfg.potentialgrid_scale);
+                    const V3 v{field[0].gx[c], field[0].gy[c], field[0].gz[c]};
+                    add_force(i, mul(mul(v, charge[i]), gs));
+                    // electrostatic_field_energy (electrostatic_field.hpp:16-23) times the scale
+                    float en = field[0].sc[c] * charge[i];
+                    en = en * C_BOLTZMANN_J_PER_K;
+                    en = en * C_JOULE_TO_KJOULE;
+                    en = en * C_AVOGADRO;
+                    pe_elec[i] += gs * en;
+                }
+            }
+            if (field[1].on)
+            {
+                // Particle::addDensityFieldForce (Particle.cpp:136-159)
+                const int64_t c = field[1].cell(x[i], y[i], z[i]);
+                if (c >= 0)
+                {
+                    const float gs = static_cast<float>(cfg.densitygrid_scale);
+                    const V3 v{field[1].gx[c], field[1].gy[c], field[1].gz[c]};
+                    add_force(i, mul(mul(v, burying.empty() ? 1.0f : burying[i]), gs));
+                }
+            }
             if (cfg.steric_enable)
                 pair_term<BS_TERM_STERIC>(i, d_steric[t]);
             if (cfg.viscosity_enable)
@@ -1010,6 +1106,36 @@ void * bso_create(const bs_config * cfg, int64_t n, const float * xyz, const flo
     s->probe.charge = static_cast<float>(cfg->probe_charge);
     s->setup_grids();
     return s;
+}
+
+// Field grid `which` (0 potential, 1 density) from its scalar values; used when the
+// configuration enables it (potentialgrid.enable with coulomb.enable, densitygrid.enable).
+void bso_set_field_grid(void * h, int32_t which, const int32_t * shape, const double * origin, const double * spacing,
+                        const float * scalar)
+{
+    auto * s = static_cast<Sim *>(h);
+    s->field[which].set(shape, origin, spacing, scalar);
+    s->field[which].on = which == 0 ? s->cfg.potentialgrid_enable != 0 : s->cfg.densitygrid_enable != 0;
+}
+
+// The grid's cells, 4 floats each (scalar, force vector).
+void bso_get_field_grid(void * h, int32_t which, float * out)
+{
+    const Field & f = static_cast<Sim *>(h)->field[which];
+    for (size_t c = 0; c < f.sc.size(); ++c)
+    {
+        out[4 * c] = f.sc[c];
+        out[4 * c + 1] = f.gx[c];
+        out[4 * c + 2] = f.gy[c];
+        out[4 * c + 3] = f.gz[c];
+    }
+}
+
+// Per-particle burying (ParticleProperty::setBurying), caller order.
+void bso_set_burying(void * h, const float * b)
+{
+    auto * s = static_cast<Sim *>(h);
+    s->burying.assign(b, b + s->n);
 }
 
 // Probe position and velocity (float[6]); zeros when the probe is off.

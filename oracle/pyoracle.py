@@ -69,10 +69,15 @@ def _bind(lib, prefix: str, cfg_type):
         "get_cells": (C.c_int, [C.c_void_p, C.c_int32, _i64p]),
     }
     sig["get_probe"] = (None, [C.c_void_p, _f32p])
+    sig["set_burying"] = (None, [C.c_void_p, _f32p])
+    if prefix == "bsref_":
+        sig["get_field_grid"] = (None, [C.c_void_p, C.c_int32, _i32p, _f32p])
     if prefix == "bso_":
         sig["set_rigid_bodies"] = (C.c_int, [C.c_void_p, C.c_int32, _i32p, _i32p])
         sig["set_velocities"] = (None, [C.c_void_p, _f32p])
         sig["eval_fp64"] = (C.c_int, [C.c_void_p, _f64p, _f64p])
+        sig["set_field_grid"] = (None, [C.c_void_p, C.c_int32, _i32p, _f64p, _f64p, _f32p])
+        sig["get_field_grid"] = (None, [C.c_void_p, C.c_int32, _f32p])
     fns = {}
     for name, (res, args) in sig.items():
         fn = getattr(lib, prefix + name)
@@ -184,6 +189,10 @@ class _CpuSim:
         self._fns["get_cells"](self.h, term, _p(out, C.c_int64))
         return out
 
+    def set_burying(self, b):
+        self._bur = np.ascontiguousarray(b, np.float32)
+        self._fns["set_burying"](self.h, _p(self._bur, C.c_float))
+
 
 class Oracle(_CpuSim):
     PREFIX = "bso_"
@@ -205,6 +214,22 @@ class Oracle(_CpuSim):
         v = np.ascontiguousarray(v, np.float32)
         self._fns["set_velocities"](self.h, _p(v, C.c_float))
 
+    def set_field_grid(self, which, scalar, origin, spacing):
+        """Grid `which` (0 potential, 1 density) from a (n0, n1, n2) array of scalar values."""
+        sc = np.ascontiguousarray(scalar, np.float32)
+        shape = np.asarray(sc.shape, np.int32)
+        o = np.asarray(origin, np.float64)
+        h = np.asarray(spacing, np.float64)
+        self._fns["set_field_grid"](self.h, int(which), _p(shape, C.c_int32), _p(o, C.c_double), _p(h, C.c_double),
+                                    _p(sc, C.c_float))
+        self._grid_shape = getattr(self, "_grid_shape", {})
+        self._grid_shape[which] = tuple(sc.shape)
+
+    def field_grid(self, which):
+        out = np.zeros(self._grid_shape[which] + (4,), np.float32)
+        self._fns["get_field_grid"](self.h, int(which), _p(out, C.c_float))
+        return out
+
     def eval_fp64(self):
         f = np.zeros((self.n, 3), np.float64)
         e = np.zeros(6, np.float64)
@@ -215,6 +240,13 @@ class Oracle(_CpuSim):
 class Reference(_CpuSim):
     PREFIX = "bsref_"
     PATH = REF_SO
+
+    def field_grid(self, which):
+        shape = np.zeros(3, np.int32)
+        self._fns["get_field_grid"](self.h, int(which), _p(shape, C.c_int32), None)
+        out = np.zeros(tuple(int(v) for v in shape) + (4,), np.float32)
+        self._fns["get_field_grid"](self.h, int(which), _p(shape, C.c_int32), _p(out, C.c_float))
+        return out
 
 
 # ---- FP64 gradient reference (adjoint_fp64.cpp) ------------------------------------------

@@ -100,6 +100,12 @@ cfgns::Configuration to_reference_config(const bs_config & c)
     conf.probe.epsilon = c.probe_epsilon;
     conf.probe.radius = c.probe_radius;
     conf.probe.charge = c.probe_charge;
+    conf.potentialgrid.enable = c.potentialgrid_enable != 0;
+    conf.potentialgrid.scale = c.potentialgrid_scale;
+    conf.potentialgrid.path = c.potentialgrid_path;
+    conf.densitygrid.enable = c.densitygrid_enable != 0;
+    conf.densitygrid.scale = c.densitygrid_scale;
+    conf.densitygrid.path = c.densitygrid_path;
     return conf;
 }
 
@@ -150,6 +156,38 @@ void * bsref_create(const bs_config * cfg, int64_t n, const float * xyz, const f
         h->rigid = true;
     }
     return h;
+}
+
+// ParticleProperty::setBurying on every caller particle.
+void bsref_set_burying(void * hp, const float * b)
+{
+    auto * h = static_cast<RefSim *>(hp);
+    for (unsigned i = 0; i < h->n; ++i)
+        h->sn.getParticle(i).setBurying(b[i]);
+}
+
+// The reference's grid (0 potential, 1 density) as read at set-up: shape and, when out is not
+// NULL, 4 floats per cell (scalar, force vector) in OpenDX order.
+void bsref_get_field_grid(void * hp, int32_t which, int32_t * shape, float * out)
+{
+    auto * h = static_cast<RefSim *>(hp);
+    const biospring::grid::PotentialGrid & g = which == 0 ? h->sn.getPotentialGrid() : h->sn.getDensityGrid();
+    for (int a = 0; a < 3; ++a)
+        shape[a] = static_cast<int32_t>(g.shape()[a]);
+    if (!out)
+        return;
+    size_t c = 0;
+    for (size_t i = 0; i < g.shape()[0]; ++i)
+        for (size_t j = 0; j < g.shape()[1]; ++j)
+            for (size_t k = 0; k < g.shape()[2]; ++k, ++c)
+            {
+                const auto & cell = g.at(biospring::grid::discrete_coordinates(
+                    {static_cast<int>(i), static_cast<int>(j), static_cast<int>(k)}));
+                out[4 * c] = cell.scalar;
+                out[4 * c + 1] = cell.vector.getX();
+                out[4 * c + 2] = cell.vector.getY();
+                out[4 * c + 3] = cell.vector.getZ();
+            }
 }
 
 void bsref_destroy(void * hp)

@@ -21,6 +21,11 @@ Fixtures:
                   SpringNetwork.cpp:281-292): positions after 20 steps
   nsearch.npz     1000 random particles in [-100, 100]^3, steric cutoff 10: the neighbour pairs
                   (src/tests/test-nsearch.cpp:103-129)
+  fields.npz      a charged 300-particle network with Coulomb under an electrostatic potential
+                  map and a density map read from OpenDX files (potentialgrid.*, densitygrid.*),
+                  per-particle burying: the reference's grid cells (scalar, force vector), forces
+                  and energies at the start, positions and energies after 1, 10 and 30 steps of a
+                  fresh handle
   probe.npz       a charged 300-particle network with LJ 12-6 Amber and Coulomb, and the probe
                   particle (probe.*, SpringNetwork.cpp:156-182) steric and electrostatic on:
                   positions, probe state and energies after 1, 10 and 30 steps
@@ -204,6 +209,69 @@ def make_probe() -> dict:
     return out
 
 
+FIELD_GRIDS = {  # which: (shape, origin, spacing, seed); part of the network lies outside each box
+    0: ((23, 19, 17), (-14.25, -12.5, -9.75), (1.5, 1.75, 1.25), 11),
+    1: ((15, 16, 14), (-18.0, -20.5, -12.0), (2.0, 2.0, 2.25), 12),
+}
+
+
+def fields_system() -> W.System:
+    s = W.ca_network(n=300, seed=5)
+    rng = np.random.default_rng(7)
+    s.charge = np.where(rng.random(s.n) < 0.3, rng.choice([-1.0, 1.0], s.n), 0.0).astype(np.float32)
+    s.config.update(coulomb_enable=1, coulomb_cutoff=12.0, coulomb_dielectric=4.0, potentialgrid_enable=1,
+                    potentialgrid_scale=1.5, densitygrid_enable=1, densitygrid_scale=0.7, timestep=0.05)
+    return s
+
+
+def make_fields() -> dict:
+    """A charged 300-particle network under an electrostatic potential map and a density map
+    (potentialgrid.*, densitygrid.*; Particle.cpp:136-189), both read by the reference's OpenDX
+    reader from files written here; per-particle burying in [0, 2)."""
+    import tempfile
+    s = fields_system()
+    rng = np.random.default_rng(8)
+    burying = rng.uniform(0.0, 2.0, s.n).astype(np.float32)
+    out: dict = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for which, (shape, origin, spacing, seed) in FIELD_GRIDS.items():
+            sc = W.field_map(shape, origin, spacing, seed, amplitude=20000.0 if which == 0 else 5000.0)
+            path = os.path.join(tmp, f"grid{which}.dx")
+            W.write_dx(path, sc, origin, spacing)
+            out[f"grid{which}"] = sc
+            out[f"grid{which}_origin"] = np.array(origin, np.float64)
+            out[f"grid{which}_spacing"] = np.array(spacing, np.float64)
+            s.config["potentialgrid_path" if which == 0 else "densitygrid_path"] = path.encode()
+        ref = po.Reference(s)
+        for key in ("potentialgrid_path", "densitygrid_path"):
+            s.config[key] = b""
+        system_arrays("in_", s, out)
+        out["burying"] = burying
+        ref.set_burying(burying)
+        out["cells0"] = ref.field_grid(0)
+        out["cells1"] = ref.field_grid(1)
+        ref.compute_forces()
+        out["forces_0"] = ref.forces()
+        out["energy_0"] = ref.energies()
+        ref.close()
+        # the trajectory from a fresh handle: the reference's force evaluation leaves its forces
+        # in the particles, where the next step would add to them
+        for key, which in (("potentialgrid_path", 0), ("densitygrid_path", 1)):
+            s.config[key] = os.path.join(tmp, f"grid{which}.dx").encode()
+        ref = po.Reference(s)
+        for key in ("potentialgrid_path", "densitygrid_path"):
+            s.config[key] = b""
+        ref.set_burying(burying)
+        done = 0
+        for mark in (1, 10, 30):
+            ref.step(mark - done)
+            done = mark
+            out[f"pos_{mark}"] = ref.positions()
+            out[f"energy_{mark}"] = ref.energies()
+        ref.close()
+    return out
+
+
 def make_nsearch() -> dict:
     rng = np.random.default_rng(1000)
     xyz = rng.uniform(-100, 100, size=(1000, 3)).astype(np.float32)
@@ -223,7 +291,7 @@ def main() -> None:
     if not po.build_reference():
         raise SystemExit("the reference sources are not present: cannot generate golden fixtures")
     makers = {"scans": None, "ca300": make_ca300, "rigid1": make_rigid, "nsearch": make_nsearch,
-              "probe": make_probe}
+              "probe": make_probe, "fields": make_fields}
     for mode in range(4):
         makers[f"mixed_m{mode}"] = (lambda m: (lambda: make_mixed(m)))(mode)
     wanted = sys.argv[1:] or list(makers)

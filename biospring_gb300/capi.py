@@ -115,6 +115,9 @@ SIGNATURES = {
                                       _f32p, _f32p, _u8p]),
     "bs_upload_springs": (C.c_int, [C.c_void_p, C.c_int64, _i32p, _f32p, _f32p]),
     "bs_set_rigid_bodies": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _i32p]),
+    "bs_load_nc": (C.c_int, [C.c_void_p, C.c_char_p, _i64p, _i64p]),
+    "bs_read_nc": (C.c_int, [C.c_char_p, _i64p, _i64p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
+                             _u8p, _i32p, _f32p, _f32p, _i32p, C.c_char_p, C.c_size_t]),
     "bs_set_field_grid": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _f64p, _f64p, _f32p]),
     "bs_read_dx": (C.c_int, [C.c_char_p, _i32p, _f64p, _f64p, _f32p, C.c_char_p, C.c_size_t]),
     "bs_get_field_grid": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _f32p]),
@@ -186,6 +189,39 @@ def default_config() -> BsConfig:
     cfg = BsConfig()
     load().bs_default_config(C.byref(cfg))
     return cfg
+
+
+def read_nc(path: str) -> dict:
+    """A BioSpring topology from a NetCDF classic file (bs_read_nc): per-particle arrays and the
+    springs; the optional arrays are None when the file does not hold them."""
+    import numpy as np
+    lib = load()
+    n = C.c_int64()
+    m = C.c_int64()
+    err = C.create_string_buffer(512)
+    nul = [None] * 13
+    rc = lib.bs_read_nc(str(path).encode(), C.byref(n), C.byref(m), *nul, err, 512)
+    if rc != BS_OK:
+        raise BsError(rc, err.value.decode())
+    f = lambda *shape: np.zeros(shape, np.float32)  # noqa: E731
+    out = dict(xyz=f(n.value, 3), mass=f(n.value), charge=f(n.value), radius=f(n.value), epsilon=f(n.value),
+               sasa=f(n.value), transfer=f(n.value), hydrophobicity=f(n.value),
+               is_static=np.zeros(n.value, np.uint8), ij=np.zeros((m.value, 2), np.int32), r0=f(m.value),
+               k=f(m.value))
+    present = np.zeros(3, np.int32)
+    p = lambda a, t: a.ctypes.data_as(C.POINTER(t))  # noqa: E731
+    rc = lib.bs_read_nc(str(path).encode(), C.byref(n), C.byref(m), p(out["xyz"], C.c_float),
+                        p(out["mass"], C.c_float), p(out["charge"], C.c_float), p(out["radius"], C.c_float),
+                        p(out["epsilon"], C.c_float), p(out["sasa"], C.c_float), p(out["transfer"], C.c_float),
+                        p(out["hydrophobicity"], C.c_float), p(out["is_static"], C.c_uint8),
+                        p(out["ij"], C.c_int32), p(out["r0"], C.c_float), p(out["k"], C.c_float),
+                        p(present, C.c_int32), err, 512)
+    if rc != BS_OK:
+        raise BsError(rc, err.value.decode())
+    for flag, key in zip(present, ("sasa", "transfer", "hydrophobicity")):
+        if not flag:
+            out[key] = None
+    return out
 
 
 def parse_msp(text: str, base: BsConfig | None = None) -> BsConfig:

@@ -12,6 +12,7 @@
 
 #include "../../include/biospring_gb300.h"
 #include "bs_field.h"
+#include "bs_nc.h"
 #include "bs_kernels.cuh"
 
 using namespace bsg;
@@ -646,6 +647,33 @@ int bs_set_rigid_bodies(bs_sim *s, int32_t nb, const int32_t *offsets, const int
     }
     s->bodies = bodies;
     s->ready = false;
+    return BS_OK;
+}
+
+int bs_load_nc(bs_sim *s, const char *path, int64_t *n_particles, int64_t *n_springs)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!path)
+        return fail(s, BS_E_ARG, "bs_load_nc: null path");
+    bsg::NcTopology t;
+    std::string msg;
+    if (!bsg::read_topology_nc(path, t, msg))
+        return fail(s, BS_E_ARG, "NetCDFReader: " + msg);
+    auto opt = [](const std::vector<float> &v) { return v.empty() ? nullptr : v.data(); };
+    int rc = bs_upload_particles(s, t.n, t.xyz.data(), nullptr, t.mass.data(), t.charge.data(), t.radius.data(),
+                                 t.epsilon.data(), opt(t.hydrophobicity), opt(t.sasa), opt(t.transfer),
+                                 t.is_static.data());
+    if (rc)
+        return rc;
+    const int64_t m = static_cast<int64_t>(t.r0.size());
+    rc = bs_upload_springs(s, m, t.ij.data(), t.r0.data(), t.k.data());
+    if (rc)
+        return rc;
+    if (n_particles)
+        *n_particles = t.n;
+    if (n_springs)
+        *n_springs = m;
     return BS_OK;
 }
 

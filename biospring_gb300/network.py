@@ -80,6 +80,15 @@ class SpringNetwork:
         self._check(self._lib.bs_upload_springs(self._h, ij.shape[0], ptr(ij, C.c_int32), ptr(r0, C.c_float),
                                                 ptr(k, C.c_float)), self._h)
 
+    def loadNetCDF(self, path: str) -> tuple:
+        """Reads a BioSpring topology (.nc, NetCDF classic) into the network, as NetCDFReader
+        does: particles and springs. Returns (particles, springs)."""
+        n = C.c_int64()
+        m = C.c_int64()
+        self._check(self._lib.bs_load_nc(self._h, str(path).encode(), C.byref(n), C.byref(m)), self._h)
+        self.n += n.value
+        return n.value, m.value
+
     # -- field grids (potentialgrid.*, densitygrid.*) ------------------------------------------
     def setFieldGrid(self, which: int, scalar, origin, spacing):
         """Map `which` (capi.BS_GRID_POTENTIAL or BS_GRID_DENSITY) from a (n0, n1, n2) array of

@@ -169,6 +169,24 @@ int bs_upload_springs(bs_sim *sim, int64_t s, const int32_t *ij, const float *eq
  * Effective when rigidbody_enable is set. */
 int bs_set_rigid_bodies(bs_sim *sim, int32_t nbodies, const int32_t *offsets, const int32_t *ids);
 
+/* Reads a BioSpring topology from a NetCDF classic file (CDF-1, CDF-2 or CDF-5) and uploads it
+ * as bs_upload_particles + bs_upload_springs would: coordinates, charges, radii, epsilon, mass (a
+ * zero mass becomes 1), dynamicstate (0: static), and when present surfaceaccessibility,
+ * hydrophobicityscale (IMPALA transfer energy) and hydrophobicity; then the springs (pairs,
+ * springsequilibrium, springsstiffness). Replaces NetCDFReader::read (src/IO/NetCDFReader.cpp:
+ * 67-203) with the same array checks and messages; NetCDF-4 (HDF5) files are BS_E_ARG.
+ * n_particles and n_springs (nullable) receive the counts read. */
+int bs_load_nc(bs_sim *sim, const char *path, int64_t *n_particles, int64_t *n_springs);
+
+/* The same topology into caller arrays, without a handle: call with NULL arrays for the counts,
+ * then with arrays of n_particles (xyz: 3 n), n_springs (ij: 2 m) entries. present (int32[3],
+ * nullable) tells whether surfaceaccessibility, hydrophobicityscale and hydrophobicity were in the
+ * file (absent arrays are left untouched). */
+int bs_read_nc(const char *path, int64_t *n_particles, int64_t *n_springs, float *xyz, float *mass, float *charge,
+               float *radius, float *epsilon, float *sasa, float *transfer, float *hydrophobicity,
+               uint8_t *is_static, int32_t *ij, float *equilibrium, float *stiffness, int32_t *present, char *err,
+               size_t err_len);
+
 /* Field grids (PotentialGrid, src/grid/PotentialGrid.hpp): which = BS_GRID_POTENTIAL or
  * BS_GRID_DENSITY. A grid of shape[0] x shape[1] x shape[2] cells of size spacing (A) from
  * origin, scalar values in OpenDX order (scalar[(i * shape[1] + j) * shape[2] + k]). The library

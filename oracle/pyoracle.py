@@ -41,6 +41,17 @@ def build_reference() -> str | None:
     return REF_SO if os.path.exists(REF_SO) else None
 
 
+def reference_dir() -> str:
+    """The reference source tree the recipe oracle/ref.mk builds from (its REF, or $REF)."""
+    if os.environ.get("REF"):
+        return os.environ["REF"]
+    with open(os.path.join(HERE, "ref.mk")) as f:
+        for line in f:
+            if line.startswith("REF ?="):
+                return line.split("=", 1)[1].strip()
+    return ""
+
+
 def have_reference() -> bool:
     return os.path.exists(REF_SO)
 

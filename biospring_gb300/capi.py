@@ -115,6 +115,8 @@ SIGNATURES = {
                                       _f32p, _f32p, _u8p]),
     "bs_upload_springs": (C.c_int, [C.c_void_p, C.c_int64, _i32p, _f32p, _f32p]),
     "bs_set_rigid_bodies": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _i32p]),
+    "bs_set_frames": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "bs_read_frames": (C.c_int, [C.c_void_p, C.c_int32, _i64p, _f32p, _f64p, _i32p, _i64p]),
     "bs_load_nc": (C.c_int, [C.c_void_p, C.c_char_p, _i64p, _i64p]),
     "bs_read_nc": (C.c_int, [C.c_char_p, _i64p, _i64p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
                              _u8p, _i32p, _f32p, _f32p, _i32p, C.c_char_p, C.c_size_t]),

@@ -2,6 +2,7 @@
 // CUDA-graph step schedule, error reporting. No torch types, no allocation on the step path.
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -68,6 +69,10 @@ struct bs_sim
         std::vector<float> cells; // 4 per cell after set-up: scalar, force vector
     } field[2];
     std::vector<float> burying; // caller order; empty: 1 for every particle
+    // frame recorder: page-locked host ring the device writes (mapped), next sequence to read
+    float *frame_xyz_h = nullptr;
+    FrameHeader *frame_hdr_h = nullptr;
+    long long frame_next = 1;
     bs_config cfg{};
     bool have_cfg = false;
     bool ready = false;
@@ -157,11 +162,26 @@ void destroy_graph(bs_sim *s)
 
 void free_growable(bs_sim *s);
 
+void free_frames(bs_sim *s)
+{
+    if (s->frame_xyz_h)
+        cudaFreeHost(s->frame_xyz_h);
+    if (s->frame_hdr_h)
+        cudaFreeHost(s->frame_hdr_h);
+    s->frame_xyz_h = nullptr;
+    s->frame_hdr_h = nullptr;
+    s->p.frame_every = 0;
+    s->p.frame_cap = 0;
+    s->p.frame_xyz = nullptr;
+    s->p.frame_hdr = nullptr;
+}
+
 void release_device(bs_sim *s)
 {
     destroy_graph(s);
     if (s->stream)
         cudaStreamSynchronize(s->stream);
+    free_frames(s);
     free_growable(s);
     s->dev.free_all();
     s->adj_dev.free_all();
@@ -674,6 +694,103 @@ int bs_load_nc(bs_sim *s, const char *path, int64_t *n_particles, int64_t *n_spr
         *n_particles = t.n;
     if (n_springs)
         *n_springs = m;
+    return BS_OK;
+}
+
+int bs_set_frames(bs_sim *s, int32_t every, int32_t capacity)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!s->ready)
+        return fail(s, BS_E_STATE, "bs_set_frames: call bs_setup first");
+    if (s->p.nsys > 0)
+        return fail(s, BS_E_STATE, "bs_set_frames: frames are recorded for single systems");
+    if (every < 0 || (every > 0 && capacity < 1))
+        return fail(s, BS_E_ARG, "bs_set_frames: every >= 0 and capacity >= 1 are required");
+    int rc = bs_synchronize(s); // no queued step may still write the old ring
+    if (rc)
+        return rc;
+    destroy_graph(s);
+    free_frames(s);
+    if (every == 0)
+        return BS_OK;
+    const size_t n3 = 3 * static_cast<size_t>(s->n);
+    BS_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&s->frame_xyz_h), sizeof(float) * n3 * capacity,
+                          cudaHostAllocMapped));
+    BS_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&s->frame_hdr_h), sizeof(FrameHeader) * capacity,
+                          cudaHostAllocMapped));
+    for (int32_t k = 0; k < capacity; ++k)
+    {
+        s->frame_hdr_h[k].seq = -2; // never a sequence number, nor "being written"
+        s->frame_hdr_h[k].step = 0;
+    }
+    Params &p = s->p;
+    BS_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&p.frame_xyz), s->frame_xyz_h, 0));
+    BS_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&p.frame_hdr), s->frame_hdr_h, 0));
+    p.frame_every = every;
+    p.frame_cap = capacity;
+    s->frame_next = s->steps_done / every + 1; // the first frame still to come
+    return BS_OK;
+}
+
+int bs_read_frames(bs_sim *s, int32_t max, int64_t *steps, float *xyz, double *energies, int32_t *count,
+                   int64_t *dropped)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!count || max < 0)
+        return fail(s, BS_E_ARG, "bs_read_frames: bad arguments");
+    *count = 0;
+    if (dropped)
+        *dropped = 0;
+    if (s->p.frame_every == 0)
+        return fail(s, BS_E_STATE, "bs_read_frames: no frames are recorded (bs_set_frames)");
+    const size_t n3 = 3 * static_cast<size_t>(s->n);
+    const int cap = s->p.frame_cap;
+    int32_t got = 0;
+    int64_t lost = 0;
+    while (got < max)
+    {
+        const long long want = s->frame_next;
+        FrameHeader *h = s->frame_hdr_h + want % cap;
+        // a sequence lock: the device sets seq to -1 before it rewrites a slot and to the frame's
+        // number after the frame is complete
+        const long long seq1 = __atomic_load_n(&h->seq, __ATOMIC_ACQUIRE);
+        if (seq1 == want)
+        {
+            const long long st = h->step;
+            double e[6];
+            for (int k = 0; k < 6; ++k)
+                e[k] = h->energies[k];
+            if (xyz)
+                std::memcpy(xyz + static_cast<size_t>(got) * n3, s->frame_xyz_h + static_cast<size_t>(want % cap) * n3,
+                            sizeof(float) * n3);
+            std::atomic_thread_fence(std::memory_order_acquire);
+            if (__atomic_load_n(&h->seq, __ATOMIC_RELAXED) != seq1)
+            {
+                ++lost; // overwritten while it was copied
+                ++s->frame_next;
+                continue;
+            }
+            if (steps)
+                steps[got] = st;
+            if (energies)
+                for (int k = 0; k < 6; ++k)
+                    energies[static_cast<size_t>(got) * 6 + k] = e[k];
+            ++got;
+            ++s->frame_next;
+        }
+        else if (seq1 > want)
+        {
+            ++lost; // the ring went round before this frame was read
+            ++s->frame_next;
+        }
+        else
+            break; // not written yet (or being written)
+    }
+    *count = got;
+    if (dropped)
+        *dropped = lost;
     return BS_OK;
 }
 
@@ -2147,7 +2264,11 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
             cudaGraph_t g = nullptr;
             BS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
             const long long before = s->launches;
+            // the adjoint's forward runs record no frames
+            const int frame_every = s->p.frame_every;
+            s->p.frame_every = 0;
             rc = record_adjoint(s, nsteps, K);
+            s->p.frame_every = frame_every;
             const cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
             if (rc)
             {

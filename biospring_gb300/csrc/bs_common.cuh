@@ -102,6 +102,16 @@ struct Ctl
     float4 probe_pos;
     float4 probe_vel;
     long long probe_steps;     // value of `steps` for which the probe last moved
+    unsigned int done_frame;   // last-block counter of the frame kernel
+};
+
+// Header of a recorded frame in the host ring: the frame's sequence number (step / every; -1
+// while it is being written), its step and the energies of that step (BS_ENERGY_* order).
+struct FrameHeader
+{
+    long long seq;
+    long long step;
+    double energies[6];
 };
 
 // State of one rigid body (RigidBody.h): position, velocity, angular momentum, orientation
@@ -244,6 +254,12 @@ struct Params
     float fg_of[2][3], fg_ih[2][3]; // origin and 1 / cell size in float, for the fast cell index
     float fg_scale[2];              // potentialgrid.scale (force and energy), densitygrid.scale
     float *bur[2];                  // per-particle burying, layout lb
+    // frame recorder (frame_every = 0: off): every frame_every steps the positions, in caller
+    // order, and the energies go to a ring of frame_cap frames in page-locked host memory that the
+    // device writes directly (mapped); headers are written last
+    int frame_every, frame_cap;
+    float *frame_xyz;               // [frame_cap][3n], device view of the host ring
+    FrameHeader *frame_hdr;         // [frame_cap]
 };
 
 constexpr int kMaxCluster = 16;

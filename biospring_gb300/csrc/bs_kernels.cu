@@ -1087,6 +1087,73 @@ int launch_ext_add(const Params &p, long long i, float fx, float fy, float fz, c
     return 1;
 }
 
+// Frame recorder, after a step (and the bodies and the probe): a frame is due when the step
+// count is a multiple of frame_every and its ring slot does not already hold it (a step that did
+// not run leaves the count, so the frame is not written twice). k_frame_open marks the slot as
+// being written; k_frame writes the positions in caller order straight into the mapped host ring
+// (one thread per particle, coalesced), and its last block writes the header after a system-wide
+// fence, so a reader that sees the header's sequence number sees the whole frame.
+__device__ __forceinline__ bool frame_due(const Params &p, long long &seq, int &slot)
+{
+    const long long st = *(volatile const long long *)&p.ctl->steps;
+    if (st <= 0 || st % p.frame_every != 0)
+        return false;
+    seq = st / p.frame_every;
+    slot = static_cast<int>(seq % p.frame_cap);
+    return *(volatile const long long *)&p.frame_hdr[slot].seq != seq;
+}
+
+__global__ void k_frame_open(Params p)
+{
+    long long seq;
+    int slot;
+    if (!frame_due(p, seq, slot))
+        return;
+    *(volatile long long *)&p.frame_hdr[slot].seq = -1;
+    __threadfence_system();
+}
+
+__global__ void __launch_bounds__(256) k_frame(Params p)
+{
+    long long seq;
+    int slot;
+    // the header of this slot is -1 while the frame is written: the decision is the same in every
+    // block, because only the last block of this launch changes it
+    const long long st = *(volatile const long long *)&p.ctl->steps;
+    if (st <= 0 || st % p.frame_every != 0)
+        return;
+    seq = st / p.frame_every;
+    slot = static_cast<int>(seq % p.frame_cap);
+    if (*(volatile const long long *)&p.frame_hdr[slot].seq != -1)
+        return;
+    Ctl *ctl = p.ctl;
+    const float4 *pos = p.pos[ctl->sbuf];
+    float *dst = p.frame_xyz + static_cast<size_t>(slot) * 3 * static_cast<size_t>(p.n);
+    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < p.n; id += gridDim.x * blockDim.x)
+    {
+        const float4 q = pos[p.inv[id]];
+        dst[3 * static_cast<size_t>(id)] = q.x;
+        dst[3 * static_cast<size_t>(id) + 1] = q.y;
+        dst[3 * static_cast<size_t>(id) + 2] = q.z;
+    }
+    __threadfence_system();
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0)
+        last = atomicAdd(&ctl->done_frame, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last || threadIdx.x != 0)
+        return;
+    __threadfence_system();
+    FrameHeader *h = p.frame_hdr + slot;
+    h->step = st;
+    for (int k = 0; k < 6; ++k)
+        h->energies[k] = ctl->energies[k];
+    __threadfence_system();
+    *(volatile long long *)&h->seq = seq;
+    ctl->done_frame = 0u;
+}
+
 int launch_step(const Params &p, int mode, cudaStream_t st)
 {
     int launched = launch_step_only(p, mode, st);
@@ -1096,6 +1163,12 @@ int launch_step(const Params &p, int mode, cudaStream_t st)
     {
         k_probe<<<1, 1024, 0, st>>>(p);
         launched += 1;
+    }
+    if (mode == MODE_STEP && p.frame_every > 0)
+    {
+        k_frame_open<<<1, 1, 0, st>>>(p);
+        k_frame<<<std::min((p.n + 255) / 256, 608), 256, 0, st>>>(p);
+        launched += 2;
     }
     return launched;
 }

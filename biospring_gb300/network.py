@@ -80,6 +80,25 @@ class SpringNetwork:
         self._check(self._lib.bs_upload_springs(self._h, ij.shape[0], ptr(ij, C.c_int32), ptr(r0, C.c_float),
                                                 ptr(k, C.c_float)), self._h)
 
+    # -- frame recorder -------------------------------------------------------------------------
+    def setFrames(self, every: int, capacity: int = 64):
+        """Records positions and energies every `every` steps into a host ring of `capacity` frames
+        that the device writes while it steps (every = 0 stops)."""
+        self._check(self._lib.bs_set_frames(self._h, int(every), int(capacity)), self._h)
+
+    def readFrames(self, max_frames: int = 1024):
+        """Complete frames, oldest first, without waiting: (steps (k,), positions (k, n, 3),
+        energies (k, 6), dropped)."""
+        steps = np.zeros(max_frames, dtype=np.int64)
+        xyz = np.zeros((max_frames, self.n, 3), dtype=np.float32)
+        en = np.zeros((max_frames, 6), dtype=np.float64)
+        cnt = C.c_int32()
+        lost = C.c_int64()
+        self._check(self._lib.bs_read_frames(self._h, int(max_frames), ptr(steps, C.c_int64), ptr(xyz, C.c_float),
+                                             ptr(en, C.c_double), C.byref(cnt), C.byref(lost)), self._h)
+        k = cnt.value
+        return steps[:k], xyz[:k], en[:k], lost.value
+
     def loadNetCDF(self, path: str) -> tuple:
         """Reads a BioSpring topology (.nc, NetCDF classic) into the network, as NetCDFReader
         does: particles and springs. Returns (particles, springs)."""

@@ -169,6 +169,20 @@ int bs_upload_springs(bs_sim *sim, int64_t s, const int32_t *ij, const float *eq
  * Effective when rigidbody_enable is set. */
 int bs_set_rigid_bodies(bs_sim *sim, int32_t nbodies, const int32_t *offsets, const int32_t *ids);
 
+/* Frame recorder (no reference counterpart; replaces the step loop's trajectory and energy writes,
+ * SpringNetwork.cpp:406, 768-779, which stop the run to copy particles): every `every` steps the
+ * device writes the positions, in caller order, and the energies of that step into a ring of
+ * `capacity` frames in page-locked host memory, without stopping the queued steps. every = 0
+ * stops recording. Call after bs_setup (a new set-up stops it). */
+int bs_set_frames(bs_sim *sim, int32_t every, int32_t capacity);
+
+/* Takes up to max complete frames, oldest first, without waiting for the device: steps[max] (the
+ * step of each frame), xyz[max * 3n] and energies[max * BS_NUM_ENERGIES] (each nullable). *count
+ * receives the frames written; *dropped (nullable) the frames lost because the ring went round
+ * before they were read. */
+int bs_read_frames(bs_sim *sim, int32_t max, int64_t *steps, float *xyz, double *energies, int32_t *count,
+                   int64_t *dropped);
+
 /* Reads a BioSpring topology from a NetCDF classic file (CDF-1, CDF-2 or CDF-5) and uploads it
  * as bs_upload_particles + bs_upload_springs would: coordinates, charges, radii, epsilon, mass (a
  * zero mass becomes 1), dynamicstate (0: static), and when present surfaceaccessibility,

@@ -297,6 +297,7 @@ def run_native(args) -> dict:
     if rank == 0 and world == 1 and not args.no_extras:
         out["batched"] = run_batched()
         out["adjoint"] = run_adjoint()
+        out["frames"] = run_frames(system)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(system, seconds=args.cpu_seconds)
     if dist is not None:
@@ -373,6 +374,46 @@ def run_batched(steps: int = 100) -> dict:
                     f"(mean degree {dbar:.1f}), linear steric 8 A, viscosity 1, dt 0.01 fs, rebuild every 10",
         "l2": "inputs larger than L2",
     }
+
+
+def run_frames(system=None, every: int = 10, steps: int = 200) -> dict:
+    """Cost of the frame recorder on the 100k workload: the same warm run with and without a frame
+    (positions in caller order and energies, written by the device into the host ring) every
+    `every` steps."""
+    import torch
+    from biospring_gb300 import SpringNetwork
+    s = system if system is not None else make_workload()
+    net = SpringNetwork()
+    net.addParticles(**{k: v for k, v in s.arrays().items() if v is not None})
+    net.addSprings(s.ij, s.r0, s.k)
+    net.setup(s.bs_config())
+    net.computeStep(2 * REBUILD)
+    stream = torch.cuda.ExternalStream(net.stream())
+
+    def timed():
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        net.synchronize()
+        a.record(stream)
+        net.computeStepAsync(steps)
+        b.record(stream)
+        net.synchronize()
+        return a.elapsed_time(b)
+
+    timed()
+    off_ms = min(timed() for _ in range(3))
+    net.setFrames(every, 4 * steps // every)
+    timed()
+    net.readFrames(4 * steps // every)
+    on_ms = min(timed() for _ in range(3))
+    got, _xyz, _en, dropped = net.readFrames(4 * steps // every)
+    net.close()
+    return {"value": s.n * steps / (on_ms * 1e-3), "unit": UNIT, "every": every,
+            "without_frames": s.n * steps / (off_ms * 1e-3), "overhead": on_ms / off_ms - 1.0,
+            "frames_read": int(len(got)), "dropped": int(dropped),
+            "bytes_per_frame": int(s.n * 12 + 64),
+            "how": "warm run of 200 steps (graph-replayed periods), CUDA events; frames go from the device "
+                   "straight into page-locked host memory"}
 
 
 def run_adjoint(reps: int = 5) -> dict:

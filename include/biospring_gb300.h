@@ -179,7 +179,8 @@ int bs_set_frames(bs_sim *sim, int32_t every, int32_t capacity);
 /* Takes up to max complete frames, oldest first, without waiting for the device: steps[max] (the
  * step of each frame), xyz[max * 3n] and energies[max * BS_NUM_ENERGIES] (each nullable). *count
  * receives the frames written; *dropped (nullable) the frames lost because the ring went round
- * before they were read. */
+ * before they were read. It may run on one other thread while the handle steps (a writer
+ * draining the ring); bs_set_frames may not. */
 int bs_read_frames(bs_sim *sim, int32_t max, int64_t *steps, float *xyz, double *energies, int32_t *count,
                    int64_t *dropped);
 

@@ -118,3 +118,30 @@ def test_frames_off_and_errors():
     with pytest.raises(BsError):
         net.readFrames()
     net.close()
+
+
+def test_frame_writer_files(tmp_path):
+    """The background writer turns the ring into a PDB trajectory and an energy table while the
+    handle steps."""
+    from biospring_gb300.trajectory import FrameWriter, enabled_terms
+    s = _system()
+    ref_pos, ref_en = _stopped(s, 10, 12)
+    net = gpu_network(s)
+    net.setFrames(10, 64)
+    terms = enabled_terms(s.config)
+    w = FrameWriter(net, str(tmp_path / "t.pdb"), str(tmp_path / "e.csv"), terms=terms)
+    for _ in range(4):
+        net.computeStep(30)
+    frames, dropped = w.close()
+    assert (frames, dropped) == (12, 0)
+    models = (tmp_path / "t.pdb").read_text().split("ENDMDL\n")[:-1]
+    assert len(models) == 12
+    for k, m in enumerate(models):
+        atoms = [ln for ln in m.splitlines() if ln.startswith("ATOM")]
+        xyz = np.array([[float(ln[30:38]), float(ln[38:46]), float(ln[46:54])] for ln in atoms])
+        assert np.abs(xyz - ref_pos[k]).max() <= 5e-4 + 1e-6
+    rows = [ln.split("\t") for ln in (tmp_path / "e.csv").read_text().splitlines()[1:]]
+    assert [int(r[0]) for r in rows] == list(range(10, 121, 10))
+    idx = [["kinetic", "spring", "steric", "electrostatic", "imp", "hydrophobic"].index(t) for t in terms]
+    np.testing.assert_array_equal(np.array([[float(v) for v in r[2:]] for r in rows]), ref_en[:, idx])
+    net.close()

@@ -329,7 +329,7 @@ __global__ void k_adj_combine(int nsp, const float *gk, const float *gr0, float 
 int launch_adj_step(const Params &p, const AdjState &a, cudaStream_t st)
 {
     // the forward step's lanes per particle (more lanes for small systems: more warps in flight)
-    const int T = p.step_lanes == 8 ? 8 : (p.step_lanes == 2 ? 2 : 4);
+    const int T = p.step_lanes >= 8 ? 8 : (p.step_lanes == 2 ? 2 : 4);
     const int nb = static_cast<int>((static_cast<long long>(p.npad) * T + kStepBlock - 1) / kStepBlock);
     if (T == 8)
         k_adj_step<8><<<nb, kStepBlock, 0, st>>>(p, a);

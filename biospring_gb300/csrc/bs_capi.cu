@@ -1058,7 +1058,7 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
         BS_CUDA(s->dev.alloc(&p.pl[t].cnt, npad));
     BS_CUDA(s->dev.alloc(&p.cell_of, npad));
     BS_CUDA(s->dev.alloc(&p.tmp_key, npad));
-    s->step_blocks = static_cast<int>((static_cast<long long>(p.n) * 8 + kStepBlock - 1) / kStepBlock);
+    s->step_blocks = static_cast<int>((static_cast<long long>(p.n) * 16 + kStepBlock - 1) / kStepBlock);
     p.blk_cap = s->step_blocks;
     BS_CUDA(s->dev.alloc(&p.blk_energy, energy_scratch_doubles(s->step_blocks)));
     BS_CUDA(cudaMemsetAsync(p.blk_energy, 0, sizeof(double) * energy_scratch_doubles(s->step_blocks), s->stream));
@@ -1347,13 +1347,13 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     p.imp_on = c.impala_enable != 0;
     p.visc_on = c.viscosity_enable != 0;
     p.steric_mode = c.steric_mode;
-    // lanes per particle: 8 for systems too small to fill the GPU with 4 (fewer than ~150 blocks
-    // of 128 threads per 100 SMs), else 4; BS_STEP_LANES overrides
-    p.step_lanes = n < 40000 ? 8 : 4;
+    // lanes per particle: the fewest of 4, 8, 16 that still give the GPU some 64-80k threads
+    // (measured: 4 lanes from 20k particles, 8 from 8k, 16 below); BS_STEP_LANES overrides
+    p.step_lanes = n >= 20000 ? 4 : (n >= 8000 ? 8 : 16);
     if (const char *env = std::getenv("BS_STEP_LANES"))
     {
         const int v = std::atoi(env);
-        if (v == 1 || v == 2 || v == 4 || v == 8)
+        if (v == 2 || v == 4 || v == 8 || v == 16)
             p.step_lanes = v;
     }
     p.dielectric_mode = c.dielectric_mode;

@@ -1043,14 +1043,14 @@ static void launch_step_lanes(const Params &p, cudaStream_t st)
     const int nb = static_cast<int>((static_cast<long long>(p.n) * threads_per + kStepKernelBlock - 1) / kStepKernelBlock);
     switch (p.step_lanes)
     {
-    case 1:
-        k_step<MODE, SM, 1><<<nb, kStepKernelBlock, 0, st>>>(p);
-        break;
     case 2:
         k_step<MODE, SM, 2><<<nb, kStepKernelBlock, 0, st>>>(p);
         break;
     case 8:
         k_step<MODE, SM, 8><<<nb, kStepKernelBlock, 0, st>>>(p);
+        break;
+    case 16:
+        k_step<MODE, SM, 16><<<nb, kStepKernelBlock, 0, st>>>(p);
         break;
     default:
         k_step<MODE, SM, 4><<<nb, kStepKernelBlock, 0, st>>>(p);

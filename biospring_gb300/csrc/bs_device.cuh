@@ -17,6 +17,18 @@ namespace
 
 __device__ __forceinline__ int status_of(const Ctl *c) { return *(volatile const int *)&c->status; }
 
+// Programmatic dependent launch: lets the next kernel of the stream begin launching now, then waits
+// until the previous kernel has completed and its writes are visible. The launch of the next
+// kernel thus overlaps this one; both instructions are no-ops for a kernel launched without the
+// programmatic-serialization attribute. Every kernel of the rebuild and step chains calls it first.
+__device__ __forceinline__ void pdl_enter()
+{
+#if BS_PDL
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+
 __device__ __forceinline__ unsigned int f2ord(float f)
 {
     const unsigned int b = __float_as_uint(f);

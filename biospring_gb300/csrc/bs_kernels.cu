@@ -48,6 +48,7 @@ namespace
 
 __global__ void __launch_bounds__(kBboxBlock) k_bbox(Params p)
 {
+    pdl_enter();
     Ctl *ctl = p.ctl;
     if (status_of(ctl) & kRebuildBlocking)
         return;
@@ -126,6 +127,7 @@ __global__ void __launch_bounds__(kBboxBlock) k_bbox(Params p)
 
 __global__ void __launch_bounds__(kBuildBlock) k_cell_count(Params p)
 {
+    pdl_enter();
     Ctl *ctl = p.ctl;
     if (status_of(ctl) & kRebuildBlocking)
         return;
@@ -148,6 +150,7 @@ __global__ void __launch_bounds__(kBuildBlock) k_cell_count(Params p)
 // (4 consecutive cells per thread) and writes the in-tile prefixes and the tile's total.
 __global__ void __launch_bounds__(1024) k_scan_tiles(Params p)
 {
+    pdl_enter();
     Ctl *ctl = p.ctl;
     if (status_of(ctl) & kRebuildBlocking)
         return;
@@ -205,6 +208,7 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(Params p)
 // the last cell.
 __global__ void __launch_bounds__(1024) k_scan_top(Params p)
 {
+    pdl_enter();
     Ctl *ctl = p.ctl;
     if (status_of(ctl) & kRebuildBlocking)
         return;
@@ -240,6 +244,7 @@ __global__ void __launch_bounds__(1024) k_scan_top(Params p)
 // rebuild.
 __global__ void __launch_bounds__(1024) k_scan_add(Params p)
 {
+    pdl_enter();
     Ctl *ctl = p.ctl;
     if (status_of(ctl) & kRebuildBlocking)
         return;
@@ -265,6 +270,7 @@ __global__ void __launch_bounds__(1024) k_scan_add(Params p)
 
 __global__ void __launch_bounds__(kBuildBlock) k_cell_place(Params p)
 {
+    pdl_enter();
     Ctl *ctl = p.ctl;
     if (status_of(ctl) & kRebuildBlocking)
         return;
@@ -285,6 +291,7 @@ __global__ void __launch_bounds__(kBuildBlock) k_cell_place(Params p)
 // no result here depends on.
 __global__ void __launch_bounds__(kBuildBlock) k_cell_sort(Params p)
 {
+    pdl_enter();
     Ctl *ctl = p.ctl;
     if (status_of(ctl) & kRebuildBlocking)
         return;
@@ -314,6 +321,7 @@ __global__ void __launch_bounds__(kBuildBlock) k_cell_sort(Params p)
 // then (last block) makes the new layout current.
 __global__ void __launch_bounds__(kBuildBlock) k_reorder(Params p)
 {
+    pdl_enter();
     Ctl *ctl = p.ctl;
     if (status_of(ctl) & kRebuildBlocking)
         return;
@@ -357,6 +365,7 @@ __global__ void __launch_bounds__(kBuildBlock) k_reorder(Params p)
 // so the row is read with contiguous loads and the partner lookups of a slot overlap.
 __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
 {
+    pdl_enter();
     Ctl *ctl = p.ctl;
     if (status_of(ctl) & kRebuildBlocking)
         return;
@@ -408,6 +417,7 @@ __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
 template <bool PL16>
 __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
 {
+    pdl_enter();
     __shared__ int sh_part[kPlWarps][kPlMaxDeg];
     __shared__ int sh_raw[kPlWarps][kPlMaxDeg];
     constexpr int kRuns = (2 * kGridDiv + 1) * (2 * kGridDiv + 1);
@@ -699,6 +709,7 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
 template <int MODE, int SM, int T>
 __global__ void __launch_bounds__(kStepKernelBlock, kStepMinBlocks) k_step(Params p)
 {
+    pdl_enter();
     Ctl *ctl = p.ctl;
     if (status_of(ctl) != 0)
         return;
@@ -741,6 +752,7 @@ __global__ void __launch_bounds__(kStepKernelBlock, kStepMinBlocks) k_step(Param
 // (Particle.cpp:109-128) and its kinetic energy, added to the step's total. One block.
 __global__ void __launch_bounds__(1024) k_probe(Params p)
 {
+    pdl_enter();
     Ctl *ctl = p.ctl;
     const long long steps = *(volatile const long long *)&ctl->steps;
     if (steps == ctl->probe_steps)
@@ -1000,6 +1012,42 @@ __global__ void __launch_bounds__(kStepBlock) k_diag_pairs(Params p, int term, l
 
 } // namespace
 
+// Launches a kernel of the rebuild or step chain; with BS_PDL set, with programmatic stream
+// serialisation, so that it may start launching while its predecessor runs (it waits in pdl_enter).
+template <typename... KArgs, typename... Args>
+static void launch_plain(void (*kern)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+                         Args &&...args)
+{
+    kern<<<grid, block, smem, st>>>(std::forward<Args>(args)...);
+}
+
+template <typename... KArgs, typename... Args>
+static void launch_chain(void (*kern)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+                         Args &&...args)
+{
+#if BS_PDL
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+#else
+    kern<<<grid, block, smem, st>>>(std::forward<Args>(args)...);
+#endif
+}
+
+#if BS_PDL_STEP
+#define BS_STEP_LAUNCH launch_chain
+#else
+#define BS_STEP_LAUNCH launch_plain
+#endif
+
 int launch_rebuild(const Params &p, cudaStream_t st)
 {
     const int nb = (p.n + kBuildBlock - 1) / kBuildBlock;
@@ -1011,18 +1059,19 @@ int launch_rebuild(const Params &p, cudaStream_t st)
     else
     {
         const int tiles = p.cell_cap / kScanTile + 1;
-        k_bbox<<<bb, kBboxBlock, 0, st>>>(p);
-        k_cell_count<<<nb, kBuildBlock, 0, st>>>(p);
-        k_scan_tiles<<<tiles, 1024, 0, st>>>(p);
-        k_scan_top<<<1, 1024, 0, st>>>(p);
-        k_scan_add<<<tiles, 1024, 0, st>>>(p);
+        launch_chain(k_bbox, bb, kBboxBlock, 0, st, p);
+        launch_chain(k_cell_count, nb, kBuildBlock, 0, st, p);
+        launch_chain(k_scan_tiles, tiles, 1024, 0, st, p);
+        launch_chain(k_scan_top, 1, 1024, 0, st, p);
+        launch_chain(k_scan_add, tiles, 1024, 0, st, p);
         launched += 5;
     }
-    k_cell_place<<<nb, kBuildBlock, 0, st>>>(p);
-    k_cell_sort<<<1216, kBuildBlock, 0, st>>>(p);
-    k_reorder<<<nb, kBuildBlock, 0, st>>>(p);
-    k_spring_ell<<<static_cast<int>((static_cast<long long>(p.npad) * kBuildLanes + kBuildBlock - 1) / kBuildBlock),
-                   kBuildBlock, 0, st>>>(p);
+    launch_chain(k_cell_place, nb, kBuildBlock, 0, st, p);
+    launch_chain(k_cell_sort, 1216, kBuildBlock, 0, st, p);
+    launch_chain(k_reorder, nb, kBuildBlock, 0, st, p);
+    launch_chain(k_spring_ell,
+                 static_cast<unsigned>((static_cast<long long>(p.npad) * kBuildLanes + kBuildBlock - 1) / kBuildBlock),
+                 kBuildBlock, 0, st, p);
     launched += 4;
     if (p.nsys > 0 || p.pl_sparse)
         return launched + launch_batch_pairlist(p, st);
@@ -1030,9 +1079,9 @@ int launch_rebuild(const Params &p, cudaStream_t st)
     // blocks past the last cell return at once)
     const int plb = p.cell_cap;
     if (p.pl16)
-        k_pairlist<true><<<plb, kPlWarps * 32, 0, st>>>(p);
+        launch_chain(k_pairlist<true>, plb, kPlWarps * 32, 0, st, p);
     else
-        k_pairlist<false><<<plb, kPlWarps * 32, 0, st>>>(p);
+        launch_chain(k_pairlist<false>, plb, kPlWarps * 32, 0, st, p);
     return launched + 1;
 }
 
@@ -1044,16 +1093,16 @@ static void launch_step_lanes(const Params &p, cudaStream_t st)
     switch (p.step_lanes)
     {
     case 2:
-        k_step<MODE, SM, 2><<<nb, kStepKernelBlock, 0, st>>>(p);
+        BS_STEP_LAUNCH(k_step<MODE, SM, 2>, nb, kStepKernelBlock, 0, st, p);
         break;
     case 8:
-        k_step<MODE, SM, 8><<<nb, kStepKernelBlock, 0, st>>>(p);
+        BS_STEP_LAUNCH(k_step<MODE, SM, 8>, nb, kStepKernelBlock, 0, st, p);
         break;
     case 16:
-        k_step<MODE, SM, 16><<<nb, kStepKernelBlock, 0, st>>>(p);
+        BS_STEP_LAUNCH(k_step<MODE, SM, 16>, nb, kStepKernelBlock, 0, st, p);
         break;
     default:
-        k_step<MODE, SM, 4><<<nb, kStepKernelBlock, 0, st>>>(p);
+        BS_STEP_LAUNCH(k_step<MODE, SM, 4>, nb, kStepKernelBlock, 0, st, p);
         break;
     }
 }
@@ -1105,6 +1154,7 @@ __device__ __forceinline__ bool frame_due(const Params &p, long long &seq, int &
 
 __global__ void k_frame_open(Params p)
 {
+    pdl_enter();
     long long seq;
     int slot;
     if (!frame_due(p, seq, slot))
@@ -1115,6 +1165,7 @@ __global__ void k_frame_open(Params p)
 
 __global__ void __launch_bounds__(256) k_frame(Params p)
 {
+    pdl_enter();
     long long seq;
     int slot;
     // the header of this slot is -1 while the frame is written: the decision is the same in every
@@ -1161,13 +1212,13 @@ int launch_step(const Params &p, int mode, cudaStream_t st)
         launched += launch_rigid(p, st); // after the step kernel, on the same stream
     if (mode == MODE_STEP && p.probe_on)
     {
-        k_probe<<<1, 1024, 0, st>>>(p);
+        BS_STEP_LAUNCH(k_probe, 1, 1024, 0, st, p);
         launched += 1;
     }
     if (mode == MODE_STEP && p.frame_every > 0)
     {
-        k_frame_open<<<1, 1, 0, st>>>(p);
-        k_frame<<<std::min((p.n + 255) / 256, 608), 256, 0, st>>>(p);
+        BS_STEP_LAUNCH(k_frame_open, 1, 1, 0, st, p);
+        BS_STEP_LAUNCH(k_frame, std::min((p.n + 255) / 256, 608), 256, 0, st, p);
         launched += 2;
     }
     return launched;

@@ -24,6 +24,15 @@ constexpr int kMaxEnergyBlocks = 1 << 16;
 
 // status bits that stop a rebuild; a stale list is what a rebuild repairs
 constexpr int kRebuildBlocking = ST_NONFINITE | ST_PAIR_CAPACITY | ST_CELL_CAPACITY | ST_WIDE;
+// Programmatic dependent launch in the rebuild chain (its eleven kernels overlap their launches:
+// 351 -> 344 us at 100k). BS_PDL_STEP extends it to the step kernels, which made the graph-replayed
+// 100k step slower (120 -> 130 us), so it is off.
+#ifndef BS_PDL
+#define BS_PDL 1
+#endif
+#ifndef BS_PDL_STEP
+#define BS_PDL_STEP 0
+#endif
 #ifndef BS_GRID_DIV
 #define BS_GRID_DIV 1
 #endif

@@ -298,6 +298,7 @@ def run_native(args) -> dict:
         out["batched"] = run_batched()
         out["adjoint"] = run_adjoint()
         out["frames"] = run_frames(system)
+        out["interactive"] = run_interactive(system)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(system, seconds=args.cpu_seconds)
     if dist is not None:
@@ -414,6 +415,37 @@ def run_frames(system=None, every: int = 10, steps: int = 200) -> dict:
             "bytes_per_frame": int(s.n * 12 + 64),
             "how": "warm run of 200 steps (graph-replayed periods), CUDA events; frames go from the device "
                    "straight into page-locked host memory"}
+
+
+def run_interactive(system=None, every: int = 10, frames: int = 50) -> dict:
+    """Interactive coupling at the 100k workload (an IMD-style loop): each frame the host pushes a
+    pulling force on 100 particles from page-locked memory, the device steps `every` steps and the
+    host reads every position back (wall clock)."""
+    import torch
+    from biospring_gb300 import SpringNetwork
+    s = system if system is not None else make_workload()
+    net = SpringNetwork()
+    net.addParticles(**{k: v for k, v in s.arrays().items() if v is not None})
+    net.addSprings(s.ij, s.r0, s.k)
+    net.setup(s.bs_config())
+    ext = torch.zeros((s.n, 3), dtype=torch.float32).pin_memory().numpy()
+    ext[:100, 0] = 1e-3
+    for _ in range(3):
+        net.setExternalForces(ext)
+        net.computeStep(every)
+        net.getPositions()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        net.setExternalForces(ext)
+        net.computeStep(every)
+        xyz = net.getPositions()
+    dt = (time.perf_counter() - t0) / frames
+    net.close()
+    assert np.isfinite(xyz).all()
+    return {"frame_rate_hz": 1.0 / dt, "ms_per_frame": dt * 1e3, "steps_per_frame": every,
+            "value": s.n * every / dt, "unit": UNIT,
+            "h2d_bytes_per_frame": int(s.n * 12 + 4), "d2h_bytes_per_frame": int(s.n * 12 + CTL_BYTES),
+            "how": "bs_set_external_forces + bs_step(every) + bs_get_positions per frame, wall clock"}
 
 
 def run_adjoint(reps: int = 5) -> dict:

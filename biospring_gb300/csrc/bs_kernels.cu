@@ -305,6 +305,30 @@ __global__ void __launch_bounds__(kBuildBlock) k_cell_sort(Params p)
     {
         const int s0 = p.cell_start[c], s1 = p.cell_start[c + 1];
         const int len = s1 - s0;
+        if (len <= 64)
+        {
+            // up to two keys per lane, ranked against every key of the cell by shuffles
+            const unsigned long long k0 = lane < len ? key[s0 + lane] : ~0ull;
+            const unsigned long long k1 = lane + 32 < len ? key[s0 + 32 + lane] : ~0ull;
+            int r0 = 0, r1 = 0;
+            for (int f = 0; f < len; ++f)
+            {
+                const unsigned long long kf = __shfl_sync(0xffffffffu, f < 32 ? k0 : k1, f & 31);
+                r0 += kf < k0;
+                r1 += kf < k1;
+            }
+            if (lane < len)
+            {
+                out[s0 + r0] = static_cast<int>(k0 & 0xffffffffu);
+                p.cell_of[s0 + r0] = c;
+            }
+            if (lane + 32 < len)
+            {
+                out[s0 + r1] = static_cast<int>(k1 & 0xffffffffu);
+                p.cell_of[s0 + r1] = c;
+            }
+            continue;
+        }
         for (int e = lane; e < len; e += 32)
         {
             const unsigned long long ke = key[s0 + e];

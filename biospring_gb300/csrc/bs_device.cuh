@@ -696,6 +696,7 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             fz = fmaf(sz, kf, fz);
             e[1] = es * p.steric_scale;
         }
+#if !BS_COUL_WARP
         if (p.coulomb_on && (fi & PF_CHARGED))
         {
             float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
@@ -705,6 +706,7 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             fz = fmaf(sz, p.k_elec_f, fz);
             e[2] = es * p.k_elec_e;
         }
+#endif
         if (p.hydro_on && (fi & PF_HYDROPHOBIC))
         {
             float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
@@ -732,6 +734,37 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
                 e[k] = 0.f;
         }
     }
+#if BS_COUL_WARP
+    // Coulomb pairs, a warp at a time: few particles are charged, so instead of a particle's own
+    // T lanes, all 32 lanes of the warp walk the row of each charged particle of the warp in turn
+    // (coalesced entries, one or two per lane), and the lead lane of that particle takes the sum.
+    if (p.coulomb_on)
+    {
+        const int lane = static_cast<int>(threadIdx.x & 31);
+        unsigned todo = __ballot_sync(0xffffffffu, lead && active && (fi & PF_CHARGED));
+        while (todo)
+        {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int sc = __shfl_sync(0xffffffffu, s, src);
+            const float4 pc = make_float4(__shfl_sync(0xffffffffu, pi.x, src), __shfl_sync(0xffffffffu, pi.y, src),
+                                          __shfl_sync(0xffffffffu, pi.z, src), __shfl_sync(0xffffffffu, pi.w, src));
+            float cx = 0.f, cy = 0.f, cz = 0.f, ce = 0.f;
+            coulomb_forces<32>(p, sc, lane, pc, p.chg[lb][sc], pos, p.chg[lb], cx, cy, cz, ce);
+            cx = group_sum<32>(cx);
+            cy = group_sum<32>(cy);
+            cz = group_sum<32>(cz);
+            ce = group_sum<32>(ce);
+            if (lane == src)
+            {
+                fx = fmaf(cx, p.k_elec_f, fx);
+                fy = fmaf(cy, p.k_elec_f, fy);
+                fz = fmaf(cz, p.k_elec_f, fz);
+                e[2] = ce * p.k_elec_e;
+            }
+        }
+    }
+#endif
     if (lead && s < send)
     {
         if (!active)

@@ -27,6 +27,11 @@ constexpr int kRebuildBlocking = ST_NONFINITE | ST_PAIR_CAPACITY | ST_CELL_CAPAC
 // Programmatic dependent launch in the rebuild chain (its eleven kernels overlap their launches:
 // 351 -> 344 us at 100k). BS_PDL_STEP extends it to the step kernels, which made the graph-replayed
 // 100k step slower (120 -> 130 us), so it is off.
+// Coulomb rows walked by the whole warp, one charged particle at a time, instead of by the
+// particle's own lanes (100k step after an L2 flush: 112.0 -> 110.8 us; warm: unchanged).
+#ifndef BS_COUL_WARP
+#define BS_COUL_WARP 1
+#endif
 #ifndef BS_PDL
 #define BS_PDL 1
 #endif

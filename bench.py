@@ -53,7 +53,7 @@ REBUILD_BYTES_PER_PARTICLE = 104.0    # key 4 + permutation 4 + gather/scatter o
 CTL_BYTES = 288                       # device control block (status, step count, energies) read per bs_step
 # DRAM bytes (read + write) of one k_step launch on this workload after an L2 flush, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum; profiles/k_step_uniform_lj_100k.md)
-STEP_KERNEL_TRAFFIC_BYTES = 77.43e6 + 2.13e6
+STEP_KERNEL_TRAFFIC_BYTES = 78.07e6 + 2.34e6
 
 
 def peaks() -> dict:

@@ -270,13 +270,16 @@ def _adj_lib():
     if _ADJ is None:
         lib = C.CDLL(ORACLE_SO)
         common = [C.c_int64, _f32p, _f32p, _f32p, _f32p, _u8p, C.c_int64, _i32p, _f32p, _f32p, C.c_double, C.c_int,
-                  C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_int32, _f32p]
+                  C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double,
+                  _f32p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int32, _f32p]
         lib.bso_loss_fp64.restype = C.c_double
         lib.bso_loss_fp64.argtypes = common
         lib.bso_adjoint_fp64.restype = C.c_int
-        lib.bso_adjoint_fp64.argtypes = common + [_f64p, _f64p, _f64p]
+        lib.bso_adjoint_fp64.argtypes = common + [_f64p, _f64p, _f64p, _f64p]
         lib.bso_fd_fp64.restype = C.c_int
         lib.bso_fd_fp64.argtypes = common + [C.c_int64, _i64p, C.c_double, _f64p, _f64p]
+        lib.bso_fd_q_fp64.restype = C.c_int
+        lib.bso_fd_q_fp64.argtypes = common + [C.c_int64, _i64p, C.c_double, _f64p]
         _ADJ = lib
     return _ADJ
 
@@ -288,13 +291,18 @@ def _adj_args(system, nsteps, target):
     keep = dict(xyz=f32(a["xyz"]).reshape(-1), vel=f32(a["vel"]), mass=f32(a["mass"]), radius=f32(a["radius"]),
                 st=None if a["is_static"] is None else np.ascontiguousarray(a["is_static"], np.uint8),
                 ij=np.ascontiguousarray(system.ij, np.int32), k=f32(system.k), r0=f32(system.r0),
-                target=f32(target).reshape(-1))
+                target=f32(target).reshape(-1), q=f32(a["charge"]))
+    # Coulomb constant C = conversion / (4 pi) * scale / dielectric (the device's k_elec_f, in double)
+    newton = 1.0e10 * (1.0 / 1.66054e-27) * 1.0e-15 * 1.0e-15
+    elec = newton * (1.60217653e-19 ** 2) / (8.854187817e-12 * 1.0e-10 * 1.0e-10) / (4.0 * 3.1415927)
+    coul_c = elec * float(cfg.coulomb_scale) / float(cfg.coulomb_dielectric)
     args = [system.n, _p(keep["xyz"], C.c_float), _p(keep["vel"], C.c_float), _p(keep["mass"], C.c_float),
             _p(keep["radius"], C.c_float), _p(keep["st"], C.c_uint8), int(system.ij.shape[0]),
             _p(keep["ij"], C.c_int32), _p(keep["k"], C.c_float), _p(keep["r0"], C.c_float), float(cfg.timestep),
             int(cfg.spring_enable), float(cfg.spring_scale), int(cfg.steric_enable), float(cfg.steric_cutoff),
-            float(cfg.steric_gridscale), int(cfg.viscosity_enable), float(cfg.viscosity_value), int(nsteps),
-            _p(keep["target"], C.c_float)]
+            float(cfg.steric_gridscale), int(cfg.viscosity_enable), float(cfg.viscosity_value),
+            _p(keep["q"], C.c_float), int(cfg.coulomb_enable), float(cfg.coulomb_cutoff), coul_c,
+            int(cfg.dielectric_mode == 1), int(nsteps), _p(keep["target"], C.c_float)]
     return args, keep
 
 
@@ -304,15 +312,28 @@ def loss_fp64(system, nsteps: int, target) -> float:
     return float(_adj_lib().bso_loss_fp64(*args))
 
 
-def adjoint_fp64(system, nsteps: int, target):
-    """(L, dL/dk, dL/dr0) by the FP64 discrete adjoint; one entry per distinct spring."""
+def adjoint_fp64(system, nsteps: int, target, with_charges: bool = False):
+    """(L, dL/dk, dL/dr0) by the FP64 discrete adjoint; one entry per distinct spring. With
+    with_charges, dL/dq of every particle is returned fourth."""
     args, _keep = _adj_args(system, nsteps, target)
     ns = system.ij.shape[0]
     gk = np.zeros(max(ns, 1), np.float64)
     gr = np.zeros(max(ns, 1), np.float64)
+    gq = np.zeros(system.n, np.float64)
     loss = C.c_double()
-    _adj_lib().bso_adjoint_fp64(*args, C.byref(loss), _p(gk, C.c_double), _p(gr, C.c_double))
+    _adj_lib().bso_adjoint_fp64(*args, C.byref(loss), _p(gk, C.c_double), _p(gr, C.c_double), _p(gq, C.c_double))
+    if with_charges:
+        return loss.value, gk[:ns], gr[:ns], gq
     return loss.value, gk[:ns], gr[:ns]
+
+
+def fd_q_fp64(system, nsteps: int, target, particles, h: float = 1e-4):
+    """Central finite differences of the FP64 loss with respect to the given particles' charges."""
+    args, _keep = _adj_args(system, nsteps, target)
+    sel = np.ascontiguousarray(particles, np.int64)
+    fq = np.zeros(sel.shape[0], np.float64)
+    _adj_lib().bso_fd_q_fp64(*args, sel.shape[0], _p(sel, C.c_int64), float(h), _p(fq, C.c_double))
+    return fq
 
 
 def fd_fp64(system, nsteps: int, target, springs, h: float = 1e-4):

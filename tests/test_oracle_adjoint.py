@@ -55,3 +55,33 @@ def test_fp64_adjoint_steric_and_mass():
     ek = np.linalg.norm(gk2[sel] - fk) / np.linalg.norm(fk)
     print(f"steric + springs, FP64 adjoint vs FD: dL/dk {ek:.2e}, dL/dr0 {er:.2e}")
     assert er < 1e-6 and ek < 1e-6
+
+
+def _charged_case(dielectric_mode: int, n=300, seed=9, steps=120):
+    s, target, steps = _case(n, seed, steps)
+    rng = np.random.default_rng(seed + 1)
+    s.charge = np.where(rng.random(n) < 0.3, rng.choice([-1.0, 1.0], n), 0.0).astype(np.float32)
+    s.config.update(coulomb_enable=1, coulomb_cutoff=12.0, coulomb_dielectric=4.0, dielectric_mode=dielectric_mode)
+    return s, target, steps
+
+
+def test_fp64_adjoint_coulomb_and_charge_gradients():
+    """Coulomb forces in the dynamics (both dielectric modes): the adjoint's spring gradients and
+    its dL/dq (charged, uncharged and static particles) against central differences."""
+    for mode in (0, 1):
+        s, target, steps = _charged_case(mode)
+        loss, gk, gr, gq = pyoracle.adjoint_fp64(s, steps, target, with_charges=True)
+        assert abs(loss - pyoracle.loss_fp64(s, steps, target)) <= 1e-14 * abs(loss)
+        sel = np.random.default_rng(2).choice(s.ij.shape[0], 16, replace=False)
+        fk, fr = pyoracle.fd_fp64(s, steps, target, sel, 1e-4)
+        ek = np.linalg.norm(gk[sel] - fk) / np.linalg.norm(fk)
+        charged = np.flatnonzero(s.charge != 0)[:8]
+        neutral = np.flatnonzero((s.charge == 0) & (s.is_static == 0))[:8]
+        fixed = np.flatnonzero(s.is_static != 0)[:4]
+        parts = np.concatenate([charged, neutral, fixed])
+        fq = pyoracle.fd_q_fp64(s, steps, target, parts, 1e-4)
+        eq = np.linalg.norm(gq[parts] - fq) / np.linalg.norm(fq)
+        print(f"mode {mode}: FP64 adjoint vs FD: dL/dk {ek:.2e}, dL/dq {eq:.2e}; |dL/dq| charged "
+              f"{np.abs(fq[:8]).mean():.2e}, neutral {np.abs(fq[8:16]).mean():.2e}, static {np.abs(fq[16:]).mean():.2e}")
+        assert ek < 1e-5 and eq < 1e-5
+        assert np.abs(fq[8:16]).max() > 0.0  # an uncharged particle's charge still matters

@@ -124,6 +124,7 @@ SIGNATURES = {
     "bs_read_dx": (C.c_int, [C.c_char_p, _i32p, _f64p, _f64p, _f32p, C.c_char_p, C.c_size_t]),
     "bs_get_field_grid": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _f32p]),
     "bs_set_burying": (C.c_int, [C.c_void_p, _f32p]),
+    "bs_set_charges": (C.c_int, [C.c_void_p, _f32p]),
     "bs_setup": (C.c_int, [C.c_void_p, C.POINTER(BsConfig)]),
     "bs_step": (C.c_int, [C.c_void_p, C.c_int32]),
     "bs_step_async": (C.c_int, [C.c_void_p, C.c_int32]),

@@ -1,5 +1,5 @@
 // bs_adjoint.cu -- discrete adjoint of the damped step, for gradients of a loss on the final
-// positions with respect to every spring's stiffness and rest length.
+// positions with respect to every spring's stiffness and rest length, and every particle's charge.
 //
 // The step being differentiated is the one the forward kernels integrate (Particle.cpp:80-84,
 // 109-128; SpringNetwork.cpp:63-198): with F_i(x) the conservative force on particle i,
@@ -16,7 +16,8 @@
 //     H w = phi'(d) (u.w) u + phi(d) / d (w - (u.w) u).
 // Springs (spring.hpp:17-29): phi = C s k (d - r0), phi' = C s k, dF_i/dk = C s (d - r0) u,
 // dF_i/dr0 = -C s k u. Linear steric overlap (steric.hpp:37-59): phi = C s' (d - (r_i + r_j)) when
-// d < r_i + r_j and the pair is within the cutoff, phi' = C s'.
+// d < r_i + r_j and the pair is within the cutoff, phi' = C s'. Coulomb (electrostatic.hpp:16-49):
+// phi = -C q_i q_j / d^2 (or -2 C q_i q_j / d^3 with eps = D r), dF_i/dq_i = (phi / q_i) u.
 //
 // Each directed spring entry (the spring seen from one end) owns two gradient accumulators, so
 // the sums need no atomics and are deterministic; the two ends are added at the end.
@@ -43,6 +44,54 @@ __device__ __forceinline__ void hvp(float phi, float dphi, float inv, float ux, 
     hx = fmaf(a, wx, fmaf(c, ux, hx));
     hy = fmaf(a, wy, fmaf(c, uy, hy));
     hz = fmaf(a, wz, fmaf(c, uz, hz));
+}
+
+// Coulomb pairs of slot s (list 1), lane t of T: the Hessian term of pairs of two charges, and
+// this step's dL/dq terms when charge gradients are asked for. With F_s = phi u, u = (x_j - x_s)/d,
+// phi = -C q_s q_j / d^2 (constant dielectric; -2 C q_s q_j / d^3 with eps = D r) and C the
+// device's Coulomb constant: dL/dq_s += (phi / q_s) u.(nu_s - nu_j), and the same with phi / q_j for
+// a static partner, which has no row of its own (added atomically). The rows list every partner
+// of the slot when charge gradients are asked for, so uncharged particles get theirs too.
+template <int T>
+__device__ __forceinline__ void adj_coulomb(const Params &p, const AdjState &a, int s, int t, int lb, float4 xi,
+                                            float4 ni, float qs, float &hx, float &hy, float &hz, float &gqs)
+{
+    const PairList &L = p.pl[1];
+    const int cnt = L.cnt[s];
+    const size_t row = static_cast<size_t>(s) * L.cap;
+    const float C = p.k_elec_f;
+    const bool dist = p.dielectric_mode == BS_DIELECTRIC_DISTANCE;
+    for (int k = t; k < cnt; k += T)
+    {
+        const unsigned int e = L.idx[row + k];
+        const int j = static_cast<int>(e & kSlotMask);
+        const bool st = (e & kEntryStatic) != 0;
+        const float4 xj = a.x[j];
+        const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (!pair_in(r2, p.lo2_c, p.hi2_c, xi, xj, p.c_coulomb, true) || r2 < 1e-6f)
+            continue;
+        const float qj = p.chg[lb][j];
+        if (qs == 0.0f && qj == 0.0f)
+            continue;
+        const float inv = rsqrt_nr(r2);
+        const float inv2 = inv * inv;
+        const float per_s = dist ? -2.0f * C * qj * inv2 * inv : -C * qj * inv2;
+        const float per_j = dist ? -2.0f * C * qs * inv2 * inv : -C * qs * inv2;
+        const float phi = per_s * qs;
+        const float dphi = (dist ? -3.0f : -2.0f) * phi * inv;
+        const float ux = dx * inv, uy = dy * inv, uz = dz * inv;
+        const float4 nj = st ? make_float4(0.f, 0.f, 0.f, 0.f) : a.nu_in[j];
+        if (phi != 0.0f)
+            hvp(phi, dphi, inv, ux, uy, uz, nj.x - ni.x, nj.y - ni.y, nj.z - ni.z, hx, hy, hz);
+        if (a.gq)
+        {
+            const float un = ux * (ni.x - nj.x) + uy * (ni.y - nj.y) + uz * (ni.z - nj.z);
+            gqs = fmaf(per_s, un, gqs);
+            if (st)
+                atomicAdd(&a.gq[p.perm[lb][j]], per_j * un);
+        }
+    }
 }
 
 // Separation xj - xi as float-float per axis, squared length r2 = (r2h, r2l), and the stretch
@@ -125,7 +174,7 @@ __global__ void __launch_bounds__(kStepBlock) k_adj_step(Params p, AdjState a)
     const bool lead = t == 0;
     const unsigned int fi = s < p.n ? p.flags[lb][s] : PF_STATIC;
     const bool active = s < p.n && !(fi & PF_STATIC);
-    float hx = 0.f, hy = 0.f, hz = 0.f;
+    float hx = 0.f, hy = 0.f, hz = 0.f, gqs = 0.f;
     float4 xi = make_float4(0.f, 0.f, 0.f, 0.f), ni = xi, li = xi;
     if (active)
     {
@@ -169,12 +218,16 @@ __global__ void __launch_bounds__(kStepBlock) k_adj_step(Params p, AdjState a)
             if (p.pl[kListStericStatic].on && p.pl[kListStericStatic].cnt[s] > 0)
                 adj_steric<T, 2>(p, a, s, t, xi, ni, hx, hy, hz);
         }
+        if (p.coulomb_on)
+            adj_coulomb<T>(p, a, s, t, lb, xi, ni, p.chg[lb][s], hx, hy, hz, gqs);
     }
     if (T > 1)
     {
         hx = group_sum<T>(hx);
         hy = group_sum<T>(hy);
         hz = group_sum<T>(hz);
+        if (a.gq)
+            gqs = group_sum<T>(gqs);
     }
     if (!lead || s >= p.npad)
         return;
@@ -183,6 +236,8 @@ __global__ void __launch_bounds__(kStepBlock) k_adj_step(Params p, AdjState a)
         a.nu_out[s] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
+    if (a.gq && p.coulomb_on)
+        a.gq[p.perm[lb][s]] += gqs;
     const float m = p.iprm[lb][s].x;
     const float b = m > 0.0f ? p.dt / m : 0.0f;
     const float av = (m > 0.0f && p.visc_on) ? 1.0f - p.visc * p.dt / m : 1.0f;

@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(kBatchPlWarps * 32) k_batch_pairlist(Params p)
         const unsigned int fi = fl[i];
         const bool dyn = !(fi & PF_STATIC);
         const bool on0 = dyn && l0;
-        const bool on1 = dyn && l1 && (fi & PF_CHARGED);
+        const bool on1 = dyn && l1 && ((fi & PF_CHARGED) || p.coul_all);
         const bool on2 = dyn && l2 && (fi & PF_HYDROPHOBIC);
         const bool need_fj = l3 || on1 || on2;
         float r2max = on0 ? r2_0 : 0.0f;
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(kBatchPlWarps * 32) k_batch_pairlist(Params p)
                     }
                     if (on1)
                     {
-                        const bool a1 = in && (fj & PF_CHARGED) && r2 < r2_1;
+                        const bool a1 = in && ((fj & PF_CHARGED) || p.coul_all) && r2 < r2_1;
                         const unsigned int m1 = __ballot_sync(0xffffffffu, a1);
                         if (a1 && cnt1 + __popc(m1 & below) < cap1)
                             row1[cnt1 + __popc(m1 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);

@@ -114,7 +114,8 @@ struct bs_sim
     double *adj_blk = nullptr, *adj_loss = nullptr;
     unsigned int *adj_done = nullptr;
     cudaGraphExec_t adj_graph = nullptr;
-    int adj_key[2] = {0, 0};
+    int adj_key[3] = {0, 0, 0};
+    float *adj_gq = nullptr; // dL/dq per caller id
     long long adj_kernels = 0;
     // diagnostics scratch
     long long *diag_out = nullptr;
@@ -185,6 +186,7 @@ void release_device(bs_sim *s)
     free_growable(s);
     s->dev.free_all();
     s->adj_dev.free_all();
+    s->adj_gq = nullptr;
     s->adj_ck_cap = 0;
     s->adj_seg_cap = 0;
     s->sp_sid_d = nullptr;
@@ -856,6 +858,29 @@ int bs_set_burying(bs_sim *s, const float *burying)
         BS_CUDA(cudaMemcpyAsync(s->staging, burying, sizeof(float) * s->n, cudaMemcpyHostToDevice, s->stream));
         s->launches += launch_set_burying(s->p, s->staging, s->stream);
         BS_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    return BS_OK;
+}
+
+int bs_set_charges(bs_sim *s, const float *charge)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!charge)
+        return fail(s, BS_E_ARG, "bs_set_charges: null argument");
+    for (int64_t i = 0; i < s->n; ++i)
+        if (!std::isfinite(charge[i]))
+            return fail(s, BS_E_ARG, "bs_set_charges: charges must be finite");
+    s->charge.assign(charge, charge + s->n);
+    if (s->ready)
+    {
+        // into the current layout, in stream order; Coulomb list membership follows the new
+        // charges from the next rebuild on, which the next step forces
+        BS_CUDA(cudaStreamSynchronize(s->stream));
+        BS_CUDA(cudaMemcpyAsync(s->staging, charge, sizeof(float) * s->n, cudaMemcpyHostToDevice, s->stream));
+        s->launches += launch_set_charges(s->p, s->staging, s->stream);
+        BS_CUDA(cudaStreamSynchronize(s->stream));
+        s->list_valid = false;
     }
     return BS_OK;
 }
@@ -2099,7 +2124,7 @@ int bs_set_spring_parameters(bs_sim *s, const float *stiffness, const float *equ
 
 // Records the whole adjoint run (forward with checkpoints, then the backward sweep with
 // recomputation from each checkpoint) on the handle's stream.
-static int record_adjoint(bs_sim *s, int nsteps, int K)
+static int record_adjoint(bs_sim *s, int nsteps, int K, bool charges)
 {
     Params &p = s->p;
     const int S = (nsteps + K - 1) / K;
@@ -2108,6 +2133,8 @@ static int record_adjoint(bs_sim *s, int nsteps, int K)
     float4 *lo_seg = p.pos_lo[0] ? s->adj_seg_lo : nullptr;
     BS_CUDA(cudaMemsetAsync(s->adj_gk, 0, sizeof(float) * 2 * std::max<size_t>(s->sp_i.size(), 1), s->stream));
     BS_CUDA(cudaMemsetAsync(s->adj_gr0, 0, sizeof(float) * 2 * std::max<size_t>(s->sp_i.size(), 1), s->stream));
+    if (charges)
+        BS_CUDA(cudaMemsetAsync(s->adj_gq, 0, sizeof(float) * s->n, s->stream));
     // forward: a checkpoint (caller order) and a rebuild at the start of every interval; the
     // positions of the last interval are kept as they are produced
     for (int seg = 0; seg < S; ++seg)
@@ -2124,7 +2151,8 @@ static int record_adjoint(bs_sim *s, int nsteps, int K)
             s->launches += launch_step(p, MODE_STEP, s->stream);
         }
     }
-    AdjState a{nullptr, nullptr, s->adj_lx, s->adj_lv, s->adj_nu[0], s->adj_nu[1], s->adj_gk, s->adj_gr0};
+    AdjState a{nullptr, nullptr, s->adj_lx, s->adj_lv, s->adj_nu[0], s->adj_nu[1], s->adj_gk, s->adj_gr0,
+               charges ? s->adj_gq : nullptr};
     s->launches += launch_adj_init(p, a, s->adj_target, s->adj_blk, s->adj_done, s->adj_loss, s->stream);
     int cur = 0;
     for (int seg = S - 1; seg >= 0; --seg)
@@ -2177,12 +2205,10 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
         return fail(s, BS_E_ARG, "bs_adjoint: nsteps >= 1, checkpoint >= 1, target and loss are required");
     if (!s->sp_i.empty() && (!dL_dk || !dL_dr0))
         return fail(s, BS_E_ARG, "bs_adjoint: dL_dk and dL_dr0 are required");
-    if (dL_dq)
-        return fail(s, BS_E_ARG, "bs_adjoint: charge gradients are not available (pass NULL)");
     const bs_config &c = s->cfg;
-    if (c.coulomb_enable || c.hydrophobicity_enable || c.impala_enable)
-        return fail(s, BS_E_ARG, "bs_adjoint: differentiates springs, linear steric and viscosity; "
-                                 "disable coulomb, hydrophobicity and impala");
+    if (c.hydrophobicity_enable || c.impala_enable)
+        return fail(s, BS_E_ARG, "bs_adjoint: differentiates springs, linear steric, Coulomb and viscosity; "
+                                 "disable hydrophobicity and impala");
     if (c.steric_enable && c.steric_mode != BS_STERIC_LINEAR)
         return fail(s, BS_E_ARG, "bs_adjoint: only the linear steric mode is differentiated");
     if (s->p.nbody > 0 || s->p.probe_on)
@@ -2195,6 +2221,19 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
     if (s->ctl_host->ext_pending)
         return fail(s, BS_E_STATE, "bs_adjoint: an external force is pending; step or clear it first");
     Params &p = s->p;
+    // charge gradients need every pair of a charged particle, so the adjoint's list builds (and a
+    // regrowth on the way) list the Coulomb partners of every dynamic particle; the flag goes
+    // back when the call returns (the next step rebuilds the lists)
+    const bool charges = dL_dq != nullptr;
+    struct CoulAll
+    {
+        Params &p;
+        int old;
+        ~CoulAll() { p.coul_all = old; }
+    } coul_all_guard{p, p.coul_all};
+    p.coul_all = charges && c.coulomb_enable ? 1 : 0;
+    if (charges && !s->adj_gq)
+        BS_CUDA(s->adj_dev.alloc(&s->adj_gq, static_cast<size_t>(s->n)));
     const int K = std::min(checkpoint, nsteps);
     const int S = (nsteps + K - 1) / K;
     const size_t n3 = 3 * static_cast<size_t>(s->n), np = static_cast<size_t>(p.npad);
@@ -2254,7 +2293,7 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
     const Ctl saved = *s->ctl_host;
     for (int attempt = 0; attempt < 4; ++attempt)
     {
-        if (!s->adj_graph || s->adj_key[0] != nsteps || s->adj_key[1] != K)
+        if (!s->adj_graph || s->adj_key[0] != nsteps || s->adj_key[1] != K || s->adj_key[2] != (charges ? 1 : 0))
         {
             if (s->adj_graph)
             {
@@ -2267,7 +2306,7 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
             // the adjoint's forward runs record no frames
             const int frame_every = s->p.frame_every;
             s->p.frame_every = 0;
-            rc = record_adjoint(s, nsteps, K);
+            rc = record_adjoint(s, nsteps, K, charges);
             s->p.frame_every = frame_every;
             const cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
             if (rc)
@@ -2284,6 +2323,7 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
                 return cuda_fail(s, ie, "bs_adjoint: cudaGraphInstantiate");
             s->adj_key[0] = nsteps;
             s->adj_key[1] = K;
+            s->adj_key[2] = charges ? 1 : 0;
             s->adj_kernels = s->launches - before;
             s->launches = before;
         }
@@ -2327,6 +2367,13 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
         {
             BS_CUDA(cudaMemcpy(dL_dk, s->adj_ok, sizeof(float) * ns, cudaMemcpyDeviceToHost));
             BS_CUDA(cudaMemcpy(dL_dr0, s->adj_or0, sizeof(float) * ns, cudaMemcpyDeviceToHost));
+        }
+        if (charges)
+        {
+            if (c.coulomb_enable)
+                BS_CUDA(cudaMemcpy(dL_dq, s->adj_gq, sizeof(float) * s->n, cudaMemcpyDeviceToHost));
+            else
+                std::memset(dL_dq, 0, sizeof(float) * s->n);
         }
         return BS_OK;
     }

@@ -193,6 +193,7 @@ struct Params
     int cell_cap;
     int *tile_sum;            // [cell_cap / kScanTile + 2] per-tile totals of the cell scan
     int pl_sparse;            // build the pair lists one warp per particle (few particles per cell)
+    int coul_all;             // list Coulomb partners of every dynamic particle, charged or not (charge gradients)
     // energies: per-block partials
     double *blk_energy;       // block and group partials of the step energies, group counters
     int blk_cap;              // block partials it holds (the step kernel's largest grid)

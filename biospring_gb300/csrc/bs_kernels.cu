@@ -529,7 +529,7 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
         const unsigned int fi = fl[i];
         const bool dyn = !(fi & PF_STATIC);
         const bool on0 = dyn && l0;
-        const bool on1 = dyn && l1 && (fi & PF_CHARGED);
+        const bool on1 = dyn && l1 && ((fi & PF_CHARGED) || p.coul_all);
         const bool on2 = dyn && l2 && (fi & PF_HYDROPHOBIC);
         const bool need_fj = l3 || on1 || on2;
         float r2max = on0 ? r2_0 : 0.0f;
@@ -617,7 +617,7 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
                 }
                 if (on1)
                 {
-                    const bool a1 = in && (fj & PF_CHARGED) && r2 < r2_1;
+                    const bool a1 = in && ((fj & PF_CHARGED) || p.coul_all) && r2 < r2_1;
                     const unsigned int m1 = __ballot_sync(0xffffffffu, a1);
                     if (a1 && cnt1 + __popc(m1 & below) < cap1)
                         row1[cnt1 + __popc(m1 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
@@ -1142,6 +1142,26 @@ __global__ void k_set_burying(Params p, const float *b)
 int launch_set_burying(const Params &p, const float *b, cudaStream_t st)
 {
     k_set_burying<<<(p.n + 255) / 256, 256, 0, st>>>(p, b);
+    return 1;
+}
+
+// New charges into the current layout (bs_set_charges): the value and the charged flag that
+// decides Coulomb list membership (the caller forces a list rebuild before the next step).
+__global__ void k_set_charges(Params p, const float *q)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id < p.n)
+    {
+        const int lb = p.ctl->lbuf, slot = p.inv[id];
+        p.chg[lb][slot] = q[id];
+        const unsigned int f = p.flags[lb][slot] & ~static_cast<unsigned int>(PF_CHARGED);
+        p.flags[lb][slot] = q[id] != 0.0f ? (f | PF_CHARGED) : f;
+    }
+}
+
+int launch_set_charges(const Params &p, const float *q, cudaStream_t st)
+{
+    k_set_charges<<<(p.n + 255) / 256, 256, 0, st>>>(p, q);
     return 1;
 }
 

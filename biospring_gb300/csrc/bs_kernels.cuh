@@ -68,6 +68,7 @@ int launch_step_only(const Params &p, int mode, cudaStream_t stream); // the ste
 int launch_rigid(const Params &p, cudaStream_t stream);               // bs_rigid.cu
 int launch_ext_add(const Params &p, long long i, float fx, float fy, float fz, cudaStream_t stream);
 int launch_set_burying(const Params &p, const float *burying, cudaStream_t stream);
+int launch_set_charges(const Params &p, const float *q, cudaStream_t st);
 int launch_unsort(const Params &p, int what, float *out3, cudaStream_t stream);
 int launch_diag_cells(const Params &p, float cutoff, float skin, uint32_t need_flag, long long *out,
                       cudaStream_t stream);
@@ -87,6 +88,7 @@ struct AdjState
     float4 *nu_out;  // the same for the step being reversed
     float *gk;       // per directed spring entry: dL/dk, dL/dr0 partial sums
     float *gr0;
+    float *gq;       // dL/dq per caller id (null: no charge gradients)
 };
 int launch_adj_step(const Params &p, const AdjState &a, cudaStream_t stream);
 int launch_adj_init(const Params &p, const AdjState &a, const float4 *target, double *blk, unsigned int *done,

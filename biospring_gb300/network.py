@@ -133,6 +133,14 @@ class SpringNetwork:
         b = _f32(burying)
         self._check(self._lib.bs_set_burying(self._h, ptr(b, C.c_float)), self._h)
 
+    def setCharges(self, charge):
+        """Replaces every particle's charge (caller order); Coulomb list membership follows at the
+        next step."""
+        q = _f32(charge)
+        if q.shape[0] != self.n:
+            raise ValueError(f"setCharges: {q.shape[0]} charges for {self.n} particles")
+        self._check(self._lib.bs_set_charges(self._h, ptr(q, C.c_float)), self._h)
+
     def setRigidBodies(self, bodies):
         offsets = np.zeros(len(bodies) + 1, dtype=np.int32)
         for b, ids in enumerate(bodies):
@@ -163,16 +171,20 @@ class SpringNetwork:
         r0 = _f32(equilibrium)
         self._check(self._lib.bs_set_spring_parameters(self._h, ptr(k, C.c_float), ptr(r0, C.c_float)), self._h)
 
-    def adjoint(self, nsteps: int, target, checkpoint: int = 20):
+    def adjoint(self, nsteps: int, target, checkpoint: int = 20, charges: bool = False):
         """Loss (1/n) sum |x(nsteps) - target|^2 and its gradient with respect to every spring's
-        stiffness and rest length, by the discrete adjoint (the state is left unchanged)."""
+        stiffness and rest length, by the discrete adjoint (the state is left unchanged). With
+        charges, dL/dq of every particle is returned fourth."""
         tg = _f32(target, (-1, 3))
         ns = self.springCount()
         gk = np.zeros(max(ns, 1), dtype=np.float32)
         gr = np.zeros(max(ns, 1), dtype=np.float32)
+        gq = np.zeros(self.n, dtype=np.float32) if charges else None
         loss = C.c_double()
         self._check(self._lib.bs_adjoint(self._h, int(nsteps), int(checkpoint), ptr(tg, C.c_float), C.byref(loss),
-                                         ptr(gk, C.c_float), ptr(gr, C.c_float), None), self._h)
+                                         ptr(gk, C.c_float), ptr(gr, C.c_float), ptr(gq, C.c_float)), self._h)
+        if charges:
+            return loss.value, gk[:ns], gr[:ns], gq
         return loss.value, gk[:ns], gr[:ns]
 
     # -- batched ensembles -----------------------------------------------------------------

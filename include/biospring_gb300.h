@@ -230,6 +230,13 @@ int bs_get_field_grid(bs_sim *sim, int32_t which, int32_t shape[3], float *out);
  * weight of the density-grid force, caller order. */
 int bs_set_burying(bs_sim *sim, const float *burying);
 
+/* Replaces every particle's charge (ParticleProperty::setCharge, ParticleProperty.h:27, for the
+ * whole array: float[n], caller order, finite), before or after bs_setup,
+ * e.g. between steps of a charge fit driven by bs_adjoint's dL_dq. A particle whose charge becomes
+ * zero leaves the Coulomb pair lists and one whose charge becomes non-zero joins them at the next
+ * step, which rebuilds the lists. */
+int bs_set_charges(bs_sim *sim, const float *charge);
+
 /* Validates the configuration, uploads everything and builds the first cell list
  * and pair list (replaces SpringNetwork::setup, SpringNetwork.cpp:646-737).
  * Cutoffs below 1e-6 for an enabled term are BS_E_ARG (SpringNetwork.cpp:667-668). */
@@ -321,13 +328,15 @@ int bs_get_spring_count(bs_sim *sim, int64_t *count);
 int bs_set_spring_parameters(bs_sim *sim, const float *stiffness, const float *equilibrium);
 
 /* Loss L = (1/n) sum_i |x_i(nsteps) - target_i|^2 after nsteps steps from the current state, and
- * its gradient with respect to every spring's stiffness (dL_dk) and rest length (dL_dr0), by the
- * discrete adjoint of the damped step with checkpoints every `checkpoint` steps and
- * recomputation in between (FP32 adjoint state). The steps run with a rebuild at every
- * checkpoint; the state, step count and energies are left as they were. Differentiates springs,
- * the linear steric mode and viscosity: Coulomb, hydrophobic and IMPALA terms are BS_E_ARG, and
- * so is a non-NULL dL_dq (charge gradients are not available). A particle that moves more than
- * half the list skin within one checkpoint interval gives BS_E_CAPACITY. target is float[3n]. */
+ * its gradient with respect to every spring's stiffness (dL_dk) and rest length (dL_dr0) and,
+ * when dL_dq is not NULL, every particle's charge (float[n], caller order; zero without
+ * coulomb.enable), by the discrete adjoint of the damped step with checkpoints every
+ * `checkpoint` steps and recomputation in between (FP32 adjoint state). The steps run with a
+ * rebuild at every checkpoint; the state, step count and energies are left as they were.
+ * Differentiates springs, the linear steric mode, Coulomb (both dielectric modes) and viscosity:
+ * hydrophobic and IMPALA terms are BS_E_ARG. Charge gradients of static particles are summed
+ * with atomics (their order is not fixed). A particle that moves more than half the list skin
+ * within one checkpoint interval gives BS_E_CAPACITY. target is float[3n]. */
 int bs_adjoint(bs_sim *sim, int32_t nsteps, int32_t checkpoint, const float *target, double *loss,
                float *dL_dk, float *dL_dr0, float *dL_dq);
 

@@ -2,7 +2,8 @@
 
 Workload: a Calpha network built as the plain CPU/GPU configuration, a target equal to the start
 positions plus a seeded smooth displacement field of 2 A, the loss after 200 damped steps with
-checkpoints every 20 steps; gradients with respect to every spring's stiffness and rest length.
+checkpoints every 20 steps; gradients with respect to every spring's stiffness and rest length,
+and, with Coulomb pairs in the dynamics, every particle's charge.
 
 At dt = 0.01 fs a step moves a particle by 1e-7 to 1e-5 A, less than half an ulp of a coordinate
 near 50 A: the reference's FP32 update x += v dt drops or rounds most of these increments, so an
@@ -137,6 +138,49 @@ def test_adjoint_parity_mode_distance_to_fp64():
     net2.close()
 
 
+@pytest.mark.parametrize("mode", [0, 1], ids=["constant", "distance"])
+def test_adjoint_coulomb_and_charge_gradients(mode):
+    """Coulomb pairs in the dynamics (30% of the particles charged, eps = 4 or 4r, some static
+    particles): spring and charge gradients against the FP64 adjoint, and dL/dq of charged,
+    uncharged and static particles against FP64 central differences."""
+    s, target, nsteps = W.adjoint_fit(2_000, seed=6, nsteps=100)
+    rng = np.random.default_rng(8)
+    s.charge = np.where(rng.random(s.n) < 0.3, rng.choice([-1.0, 1.0], s.n), 0.0).astype(np.float32)
+    s.is_static = np.zeros(s.n, np.uint8)
+    s.is_static[::53] = 1
+    s.config.update(coulomb_enable=1, coulomb_cutoff=12.0, coulomb_dielectric=4.0, dielectric_mode=mode,
+                    precise_positions=1)
+    net = gpu_network(s)
+    loss, gk, gr, gq = net.adjoint(nsteps, target, checkpoint=20, charges=True)
+    ref_loss, rk, rr, rq = pyoracle.adjoint_fp64(s, nsteps, target, with_charges=True)
+    print(f"Coulomb mode {mode}: loss rel {abs(loss - ref_loss) / ref_loss:.2e}; vs FP64 adjoint: "
+          f"dL/dk {rel(gk, rk):.2e}, dL/dr0 {rel(gr, rr):.2e}, dL/dq {rel(gq, rq):.2e}")
+    assert abs(loss - ref_loss) <= 1e-6 * abs(ref_loss)
+    assert rel(gk, rk) < GRAD_TOL and rel(gr, rr) < GRAD_TOL and rel(gq, rq) < GRAD_TOL
+    parts = np.concatenate([np.flatnonzero(s.charge != 0)[:8],
+                            np.flatnonzero((s.charge == 0) & (s.is_static == 0))[:8],
+                            np.flatnonzero(s.is_static != 0)[:4]])
+    fq = pyoracle.fd_q_fp64(s, nsteps, target, parts, 1e-4)
+    print(f"20 charges vs FP64 central differences: {rel(gq[parts], fq):.2e} (FP64 adjoint {rel(rq[parts], fq):.2e})")
+    assert rel(gq[parts], fq) < GRAD_TOL
+    # new charges (a charge fit's update; some particles change between charged and neutral)
+    q2 = (s.charge + 0.1 * rng.standard_normal(s.n) * (rng.random(s.n) < 0.5)).astype(np.float32)
+    net.setCharges(q2)
+    loss2, gk2, gr2, gq2 = net.adjoint(nsteps, target, checkpoint=20, charges=True)
+    s.charge = q2
+    ref2 = pyoracle.adjoint_fp64(s, nsteps, target, with_charges=True)
+    print(f"after setCharges: loss rel {abs(loss2 - ref2[0]) / ref2[0]:.2e}; dL/dk {rel(gk2, ref2[1]):.2e}, "
+          f"dL/dq {rel(gq2, ref2[3]):.2e}")
+    assert abs(loss2 - ref2[0]) <= 1e-6 * abs(ref2[0])
+    assert rel(gk2, ref2[1]) < GRAD_TOL and rel(gr2, ref2[2]) < GRAD_TOL and rel(gq2, ref2[3]) < GRAD_TOL
+    # the state is untouched and the forward path still steps
+    x0 = net.getPositions()
+    net.adjoint(nsteps, target, checkpoint=20)
+    assert net.getPositions().tobytes() == x0.tobytes()
+    net.computeStep(5)
+    net.close()
+
+
 def test_adjoint_rejections():
     s, target, nsteps = W.adjoint_fit(500, seed=2, nsteps=20)
     lj = dict(s.config, steric_mode=1)
@@ -174,4 +218,37 @@ def test_fit_harness_descends():
     print("fit losses", losses)
     assert all(b < a for a, b in zip(losses, losses[1:]))
     assert k.grad is not None and r0.grad is not None
+    net.close()
+
+
+def test_fit_harness_charges_descend():
+    """Charges as the fitted tensor: the target is the end state of the same network with other
+    charges, and plain gradient descent on q lowers the loss at every step."""
+    torch = pytest.importorskip("torch")
+    from biospring_gb300.fit import SpringFitLoss
+    s, _, nsteps = W.adjoint_fit(1_000, seed=5, nsteps=40)
+    rng = np.random.default_rng(12)
+    q_true = np.where(rng.random(s.n) < 0.4, rng.choice([-1.0, 1.0], s.n), 0.0).astype(np.float32)
+    s.charge = q_true
+    s.config.update(timestep=0.5, coulomb_enable=1, coulomb_cutoff=12.0, coulomb_dielectric=1.0, dielectric_mode=0)
+    net = gpu_network(s)
+    x0 = net.getPositions()
+    net.setVelocities(np.zeros_like(x0))
+    net.computeStep(nsteps)
+    target = net.getPositions()
+    net.setPositions(x0)
+    net.setVelocities(np.zeros_like(x0))
+    k = torch.tensor(s.k)
+    r0 = torch.tensor(s.r0)
+    q = torch.tensor(q_true * 0.5, requires_grad=True)
+    losses = []
+    for _ in range(4):
+        loss = SpringFitLoss.apply(k, r0, net, target, nsteps, 20, q)
+        loss.backward()
+        losses.append(float(loss.detach()))
+        with torch.no_grad():  # a fixed-length step along the negative gradient
+            q -= 0.5 * q.grad / q.grad.norm()
+        q.grad = None
+    print("charge fit losses", losses)
+    assert all(b < a for a, b in zip(losses, losses[1:]))
     net.close()

@@ -179,6 +179,38 @@ def test_distance_dielectric_against_fp64():
     assert rel_scalar(e[3], e64[3]) < 1e-5
 
 
+def test_charges_after_setup():
+    """bs_set_charges after a few steps (the layout already permuted): a fifth of the particles
+    change between charged and neutral. Forces within the force bar of the oracle built with the
+    new charges at the same state, the Coulomb pair set bit-exact, then three steps in step."""
+    import dataclasses
+    g = load_golden("mixed_m1.npz")
+    s = system_from_golden(g)
+    net = gpu_network(s)
+    net.computeStep(2)
+    rng = np.random.default_rng(3)
+    q2 = s.charge.astype(np.float32).copy()
+    flip = rng.random(s.n) < 0.2
+    q2[flip] = np.where(q2[flip] == 0.0, rng.choice([-1.0, 0.5], s.n)[flip], 0.0)
+    net.setCharges(q2)
+    net.computeForces()
+    s2 = dataclasses.replace(s, xyz=net.getPositions(), vel=net.getVelocities(), charge=q2)
+    orc = po.Oracle(s2)
+    orc.compute_forces()
+    fo = orc.forces()
+    tol, own = force_tolerance(s2, fo)
+    err = rel_l2(net.getForces(), fo, dynamic_mask(s2))
+    print(f"{int(flip.sum())} charges changed: force rel err {err:.3e} (oracle vs FP64 {own:.3e})")
+    assert err <= tol
+    np.testing.assert_array_equal(net.getPairs(1), orc.pairs(1).astype(np.int64))
+    assert rel_scalar(net.energies()["electrostatic"], orc.energies()[3]) < 1e-5
+    net.computeStep(3)
+    orc.step(3)
+    assert np.abs(net.getPositions() - orc.positions()).max() < 1e-4
+    net.close()
+    orc.close()
+
+
 def test_long_trajectory_tracks_oracle():
     """2,000-particle Calpha network, 200 damped steps (the plain CPU/GPU configuration)."""
     from biospring_gb300 import workloads as W

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kBatchBboxBlock) k_batch_bbox(Params p)
             ok = ok && isfinite(mn[k]) && isfinite(mx[k]) && mn[k] <= mx[k];
         }
         SysGrid g;
-        g.radius = p.list_radius / static_cast<float>(kGridDiv);
+        g.radius = p.list_radius / static_cast<float>(kSparseDiv);
         int nc[3] = {1, 1, 1};
         double gmin[3] = {0.0, 0.0, 0.0};
         double cells = ok ? grid_dims(mn, mx, g.radius, gmin, nc) : 1.0;
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(1024) k_batch_cell_scan(Params p)
 
 // Typed pair lists, one warp per home particle: the rules of the cell-block build (every pair
 // within the list radius of its term, the slot itself and spring partners excluded, static
-// partners of the steric term apart); the warp walks the (2 kGridDiv + 1)^2 contiguous x-runs of
+// partners of the steric term apart); the warp walks the (2 kSparseDiv + 1)^2 contiguous x-runs of
 // the neighbour cells, 32 candidates per pass, and a ballot appends the accepted ones to the row
 // in ascending slot order. Used for batched ensembles (BATCH: each system's own grid) and for
 // sparse single systems (a few particles per cell or fewer), where one block per cell would
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(kBatchPlWarps * 32) k_batch_pairlist(Params p)
     const size_t stride = static_cast<size_t>(p.npad);
     const unsigned int below = (1u << lane) - 1u;
     int *part = sh_part[wid];
-    constexpr int kSpan = 2 * kGridDiv + 1;
+    constexpr int kSpan = 2 * kSparseDiv + 1;
     for (int i = blockIdx.x * kBatchPlWarps + wid; i < p.n; i += gridDim.x * kBatchPlWarps)
     {
         const unsigned int fi = fl[i];
@@ -276,13 +276,13 @@ __global__ void __launch_bounds__(kBatchPlWarps * 32) k_batch_pairlist(Params p)
             unsigned int *row3 = p.pl[3].idx + static_cast<size_t>(i) * cap3;
             for (int r = 0; r < kSpan * kSpan; ++r)
             {
-                const int y = cy + r % kSpan - kGridDiv;
-                const int z = cz + r / kSpan - kGridDiv;
+                const int y = cy + r % kSpan - kSparseDiv;
+                const int z = cz + r / kSpan - kSparseDiv;
                 if (y < 0 || y >= ny || z < 0 || z >= nz)
                     continue;
                 const int rowc = cbase + (z * ny + y) * nx;
-                const int j0 = p.cell_start[rowc + max(cx - kGridDiv, 0)];
-                const int j1 = p.cell_start[rowc + min(cx + kGridDiv, nx - 1) + 1];
+                const int j0 = p.cell_start[rowc + max(cx - kSparseDiv, 0)];
+                const int j1 = p.cell_start[rowc + min(cx + kSparseDiv, nx - 1) + 1];
                 for (int jb = j0; jb < j1; jb += 32)
                 {
                     const int j = jb + lane;

@@ -1117,7 +1117,9 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     p.list_radius = static_cast<float>(list_radius);
     // grid cells and density from the bounding box of each system (one system unless batched)
     const int nsys = batch ? static_cast<int>(s->sys_off.size() - 1) : 1;
-    double cells = 0.0, density = 0.0;
+    // cells of the list radius (warp-per-particle build, batches) and of a kGridDiv-th of it
+    // (cell-block build)
+    double cells1 = 0.0, cells_div = 0.0, density = 0.0;
     for (int b = 0; b < nsys; ++b)
     {
         const int64_t i0 = batch ? s->sys_off[b] : 0, i1 = batch ? s->sys_off[b + 1] : n;
@@ -1128,19 +1130,22 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
                 lo[k] = std::min(lo[k], static_cast<double>(s->xyz[3 * i + k]));
                 hi[k] = std::max(hi[k], static_cast<double>(s->xyz[3 * i + k]));
             }
-        double c3 = 1.0, volume = 1.0;
+        double c1 = 1.0, cd = 1.0, volume = 1.0;
         for (int k = 0; k < 3; ++k)
         {
-            c3 *= std::ceil((hi[k] - lo[k]) / (list_radius / kGridDiv)) + 3.0;
+            c1 *= std::ceil((hi[k] - lo[k]) / (list_radius / kSparseDiv)) + 3.0;
+            cd *= std::ceil((hi[k] - lo[k]) / (list_radius / kGridDiv)) + 3.0;
             volume *= std::max(hi[k] - lo[k], 1.0);
         }
-        cells += c3;
+        cells1 += c1;
+        cells_div += cd;
         density = std::max(density, static_cast<double>(i1 - i0) / volume);
     }
+    // fewer than ~8 particles per cell of the list radius: one warp per particle builds the lists
+    // faster than one block per (mostly empty) group of cells
+    p.pl_sparse = static_cast<double>(n) < 8.0 * cells1 ? 1 : 0;
+    const double cells = batch || p.pl_sparse ? cells1 : cells_div;
     const int cell_cap = static_cast<int>(std::min(2.0 * cells + 1024.0, 2.0e8));
-    // fewer than ~8 particles per cell: one warp per particle builds the lists faster than one
-    // block per (mostly empty) cell
-    p.pl_sparse = static_cast<double>(n) < 8.0 * cells ? 1 : 0;
     // first capacity: 1.5x the mean count expected in the list sphere, at least 32
     int caps[kLists];
     for (int t = 0; t < kLists; ++t)

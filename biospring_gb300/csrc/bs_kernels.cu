@@ -104,7 +104,9 @@ __global__ void __launch_bounds__(kBboxBlock) k_bbox(Params p)
         enc[k] = 0xffffffffu; // reset for the next rebuild
         enc[3 + k] = 0u;
     }
-    const float edge = p.list_radius / static_cast<float>(kGridDiv);
+    // the cell-block list build uses cells of a kGridDiv-th of the list radius, the warp-per-particle
+    // build (sparse systems) cells of the list radius
+    const float edge = p.list_radius / static_cast<float>(p.pl_sparse ? kSparseDiv : kGridDiv);
     int nc[3];
     double gmin[3];
     const double cells = grid_dims(mn, mx, edge, gmin, nc);
@@ -425,93 +427,54 @@ __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
 // static partners apart), Coulomb (both charged) and hydrophobic (both hydrophobic), minus the
 // slot itself and, when springs are enabled, its spring partners (Particle.cpp:213-218).
 //
-// A block owns one cell and its kPlWarps warps share the cell's home particles (warp w takes
-// every kPlWarps-th one). The grid edge is (cutoff + skin) / kGridDiv, so the neighbourhood is a
-// (2 kGridDiv + 1)^3 block of cells, i.e. (2 kGridDiv + 1)^2 contiguous x-runs of slots, staged
-// in shared memory. Cells are x-sorted, so each run is one x-sorted sequence: for one home
-// particle at a time, lane r bounds run r by binary search to the x-interval the list radius
-// allows at that run's y/z distance, and the warp walks the bounded runs, 32 candidates per
-// pass, one per lane. Accepted candidates are found with one ballot and appended to the home
-// particle's row-major row at consecutive positions (coalesced stores); the home particle's
-// state stays in registers and lanes never diverge. Rows come out in ascending slot order.
-// Bonded partners are excluded with the home particle's spring partners, sorted in shared
-// memory, which each lane walks with its own pointer (its candidates ascend). A cell whose
-// neighbourhood exceeds the stage reads whole runs from global memory. In 16-bit mode the
-// steric row holds partner-minus-slot offsets.
+// The grid edge is (cutoff + skin) / kGridDiv, so a particle's neighbours lie within kGridDiv
+// cells in each direction: in (2 kGridDiv + 1)^2 x-runs of cells, each a contiguous range of
+// slots. A block owns a group of kGridDiv^3 cells (grid-stride over the groups) and stages in
+// shared memory the x-runs that cover the group's neighbourhood, (3 kGridDiv)^2 rows of
+// 3 kGridDiv cells; its kPlWarps warps share the group's home particles. Cells are x-sorted and
+// a cell's index grows with x, so every staged row is one x-sorted sequence: for one home particle
+// at a time, lane r bounds the home's run r by binary search to the x-interval the list radius
+// allows at that run's y/z distance. With kGridDiv > 1 the bounded runs are walked as one packed
+// sequence (every window full but the last), else run by run; 32 candidates per pass, one per
+// lane. Accepted candidates are found with one ballot and appended to the home particle's
+// row-major row at consecutive positions (coalesced stores); the home particle's state stays in
+// registers and lanes never diverge. Rows come out in ascending slot order (runs ascend in z, then
+// y; slots ascend within a run). Bonded partners are excluded without touching memory in the
+// windows: the home's spring partners sit in registers (two per lane), each lane maps its partners
+// once to their positions in the candidate sequence (runs are contiguous slot ranges), and a
+// window's excluded lanes come from one OR-reduction over the warp. A group whose neighbourhood exceeds the stage reads whole rows from global memory. In
+// 16-bit mode the steric row holds partner-minus-slot offsets.
 template <bool PL16>
-__global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
+__global__ void __launch_bounds__(kPlWarps * 32, kPlMinBlocks) k_pairlist(Params p)
 {
     pdl_enter();
-    __shared__ int sh_part[kPlWarps][kPlMaxDeg];
-    __shared__ int sh_raw[kPlWarps][kPlMaxDeg];
-    constexpr int kRuns = (2 * kGridDiv + 1) * (2 * kGridDiv + 1);
-    __shared__ int sh_run[kRuns][3]; // first slot, end slot, offset in the stage
+    constexpr int kD = kGridDiv;        // neighbours lie within kD cells
+    constexpr int kG = kGridDiv;        // a block's group is kG^3 cells
+    constexpr int kSpan = 2 * kD + 1;   // a home particle's runs per dimension (y, z)
+    constexpr int kRuns = kSpan * kSpan;
+    constexpr int kRowsD = kG + 2 * kD; // staged rows per dimension (y, z)
+    constexpr int kRows = kRowsD * kRowsD;
+    constexpr int kStageUnroll = 4;
+    static_assert(kRuns <= 32, "one lane per x-run");
+    __shared__ int sh_row[kRows][3];     // first slot, end slot, offset in the stage
+    __shared__ int sh_home[kG * kG][3];  // the group's home x-runs: first slot, end slot, first home
+#if BS_PL_PACK
+    __shared__ int sh_cr[kPlWarps][2 * kRuns]; // per warp: the non-empty runs' stage index and first k
+#endif
     __shared__ float4 sh_pos[kPlStage];
     __shared__ int sh_slot[kPlStage];
     __shared__ unsigned char sh_flag[kPlStage];
-    __shared__ int blocked, staged;
+    __shared__ int blocked, staged, n_home, n_stage;
     Ctl *ctl = p.ctl;
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nx = ctl->gnx, ny = ctl->gny, nz = ctl->gnz;
-    const int c = blockIdx.x;
     if (threadIdx.x == 0)
-        blocked = (status_of(ctl) & kRebuildBlocking) || c >= nx * ny * nz;
+        blocked = (status_of(ctl) & kRebuildBlocking) != 0;
     __syncthreads();
     if (blocked)
         return;
-    const int h0 = p.cell_start[c], h1 = p.cell_start[c + 1];
-    if (h0 == h1)
-        return;
-    const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
-    if (threadIdx.x < kRuns)
-    {
-        constexpr int w = 2 * kGridDiv + 1;
-        const int y = cy + static_cast<int>(threadIdx.x % w) - kGridDiv;
-        const int z = cz + static_cast<int>(threadIdx.x / w) - kGridDiv;
-        int j0 = 0, j1 = 0;
-        if (y >= 0 && y < ny && z >= 0 && z < nz)
-        {
-            const int base = (z * ny + y) * nx;
-            j0 = p.cell_start[base + max(cx - kGridDiv, 0)];
-            j1 = p.cell_start[base + min(cx + kGridDiv, nx - 1) + 1];
-        }
-        sh_run[threadIdx.x][0] = j0;
-        sh_run[threadIdx.x][1] = j1;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0)
-    {
-        int tot = 0, lo = h0, hi = h1;
-        for (int r = 0; r < kRuns; ++r)
-        {
-            sh_run[r][2] = tot;
-            const int len = sh_run[r][1] - sh_run[r][0];
-            tot += len;
-            if (len > 0)
-            {
-                lo = min(lo, sh_run[r][0]);
-                hi = max(hi, sh_run[r][1]);
-            }
-        }
-        staged = tot <= kPlStage;
-        // every candidate offset of this cell fits 16 bits, or the list goes 32-bit
-        if (PL16 && (hi - 1 - h0 > 32767 || lo - (h1 - 1) < -32768))
-            atomicOr(&ctl->status, ST_WIDE);
-    }
-    __syncthreads();
-    // the candidate positions of the 27 cells are read by every warp of the block: stage them
-    if (staged)
-        for (int r = 0; r < kRuns; ++r)
-        {
-            const int j0 = sh_run[r][0], len = sh_run[r][1] - j0, o = sh_run[r][2];
-            for (int k = threadIdx.x; k < len; k += blockDim.x)
-            {
-                sh_pos[o + k] = p.pos[ctl->sbuf][j0 + k];
-                sh_slot[o + k] = j0 + k;
-                sh_flag[o + k] = static_cast<unsigned char>(p.flags[ctl->lbuf][j0 + k]);
-            }
-        }
-    __syncthreads();
+    const int nx = ctl->gnx, ny = ctl->gny, nz = ctl->gnz;
+    const int ngx = (nx + kG - 1) / kG, ngy = (ny + kG - 1) / kG, ngz = (nz + kG - 1) / kG;
+    const int ngroups = ngx * ngy * ngz;
     const int sb = ctl->sbuf, lb = ctl->lbuf;
     const float4 *__restrict__ pos = p.pos[sb];
     const unsigned int *__restrict__ fl = p.flags[lb];
@@ -523,203 +486,383 @@ __global__ void __launch_bounds__(kPlWarps * 32) k_pairlist(Params p)
     const int cap0 = p.pl[0].cap, cap1 = p.pl[1].cap, cap2 = p.pl[2].cap, cap3 = p.pl[3].cap;
     const size_t stride = static_cast<size_t>(p.npad);
     const unsigned int below = (1u << lane) - 1u;
-    int *part = sh_part[wid];
-    for (int i = h0 + wid; i < h1; i += kPlWarps)
+    for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x)
     {
-        const unsigned int fi = fl[i];
-        const bool dyn = !(fi & PF_STATIC);
-        const bool on0 = dyn && l0;
-        const bool on1 = dyn && l1 && ((fi & PF_CHARGED) || p.coul_all);
-        const bool on2 = dyn && l2 && (fi & PF_HYDROPHOBIC);
-        const bool need_fj = l3 || on1 || on2;
-        float r2max = on0 ? r2_0 : 0.0f;
-        if (on1)
-            r2max = fmaxf(r2max, r2_1);
-        if (on2)
-            r2max = fmaxf(r2max, r2_2);
-        int cnt0 = 0, cnt1 = 0, cnt2 = 0, cnt3 = 0;
-        if (on0 || on1 || on2)
+        const int gx0 = grp % ngx * kG, gy0 = grp / ngx % ngy * kG, gz0 = grp / (ngx * ngy) * kG;
+        const int xa = max(gx0 - kD, 0), xb = min(gx0 + kG - 1 + kD, nx - 1), hxb = min(gx0 + kG - 1, nx - 1);
+        __syncthreads(); // the previous group's stage and tables are no longer read
+        for (int t = threadIdx.x; t < kRows + kG * kG; t += blockDim.x)
         {
-            const float4 pi = pos[i];
-            // spring partners of i, sorted ascending in shared memory (rank sort across the warp)
-            const int deg = p.spring_on ? p.se_deg[i] : 0;
-            const bool small = deg <= kPlMaxDeg;
-            __syncwarp();
-            if (small)
+            int j0 = 0, j1 = 0;
+            if (t < kRows)
             {
-                int *raw = sh_raw[wid];
-                for (int k = lane; k < deg; k += 32)
-                    raw[k] = static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask);
-                __syncwarp();
-                for (int k = lane; k < deg; k += 32)
+                const int y = gy0 - kD + t % kRowsD, z = gz0 - kD + t / kRowsD;
+                if (y >= 0 && y < ny && z >= 0 && z < nz)
                 {
-                    const int v = raw[k];
-                    int rank = 0;
-                    for (int m = 0; m < deg; ++m)
-                    {
-                        const int w = raw[m];
-                        rank += (w < v) || (w == v && m < k);
-                    }
-                    part[rank] = v;
+                    const int base = (z * ny + y) * nx;
+                    j0 = p.cell_start[base + xa];
+                    j1 = p.cell_start[base + xb + 1];
                 }
-            }
-            __syncwarp();
-            int bp = 0;
-            short *row0s = reinterpret_cast<short *>(p.pl[0].idx) + static_cast<size_t>(i) * cap0;
-            unsigned int *row0 = p.pl[0].idx + static_cast<size_t>(i) * cap0;
-            unsigned int *row1 = p.pl[1].idx + static_cast<size_t>(i) * cap1;
-            unsigned int *row2 = p.pl[2].idx + static_cast<size_t>(i) * cap2;
-            unsigned int *row3 = p.pl[3].idx + static_cast<size_t>(i) * cap3;
-            // One window of up to 32 candidates, one per lane. Each lane sees its candidates in
-            // ascending slot order over the windows, so it walks the sorted spring partners with
-            // its own pointer bp (at most deg steps over the whole scan).
-            auto window = [&](const int j, const bool jv, const float4 pj, const unsigned int fj) {
-                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                bool in = jv && r2 < r2max && j != i;
-                if (deg)
-                {
-                    if (small)
-                    {
-                        while (bp < deg && part[bp] < j)
-                            ++bp;
-                        in = in && !(bp < deg && part[bp] == j);
-                    }
-                    else
-                        for (int k = 0; k < deg; ++k)
-                            in = in && static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask) != j;
-                }
-                const bool st = (fj & PF_STATIC) != 0;
-                if (on0)
-                {
-                    const bool a0 = in && !st && r2 < r2_0;
-                    const unsigned int m0 = __ballot_sync(0xffffffffu, a0);
-                    if (a0)
-                    {
-                        const int at = cnt0 + __popc(m0 & below);
-                        if (at < cap0)
-                        {
-                            if (PL16)
-                                row0s[at] = static_cast<short>(j - i);
-                            else
-                                row0[at] = static_cast<unsigned int>(j);
-                        }
-                    }
-                    cnt0 += __popc(m0);
-                    if (l3)
-                    {
-                        const bool a3 = in && st && r2 < r2_0;
-                        const unsigned int m3 = __ballot_sync(0xffffffffu, a3);
-                        if (a3 && cnt3 + __popc(m3 & below) < cap3)
-                            row3[cnt3 + __popc(m3 & below)] = static_cast<unsigned int>(j) | kEntryStatic;
-                        cnt3 += __popc(m3);
-                    }
-                }
-                if (on1)
-                {
-                    const bool a1 = in && ((fj & PF_CHARGED) || p.coul_all) && r2 < r2_1;
-                    const unsigned int m1 = __ballot_sync(0xffffffffu, a1);
-                    if (a1 && cnt1 + __popc(m1 & below) < cap1)
-                        row1[cnt1 + __popc(m1 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
-                    cnt1 += __popc(m1);
-                }
-                if (on2)
-                {
-                    const bool a2 = in && (fj & PF_HYDROPHOBIC) && r2 < r2_2;
-                    const unsigned int m2 = __ballot_sync(0xffffffffu, a2);
-                    if (a2 && cnt2 + __popc(m2 & below) < cap2)
-                        row2[cnt2 + __popc(m2 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
-                    cnt2 += __popc(m2);
-                }
-            };
-            if (staged)
-            {
-                // Each run is x-sorted: lane r bounds run r to the candidates whose x lies within
-                // the list radius of the home particle, given the run's distance in y and z
-                // (cell bounds widened by kRowMargin, the grid's outer cells unbounded), by binary
-                // search. Every candidate inside the bounds is still tested exactly; those outside
-                // are farther than the radius. The warp then walks the bounded runs in order.
-                int lo_r = 0, cnt_r = 0;
-                if (lane < kRuns)
-                {
-                    const int j0 = sh_run[lane][0], len = sh_run[lane][1] - j0, o = sh_run[lane][2];
-                    if (len > 0)
-                    {
-                        const int ry = cy + lane % (2 * kGridDiv + 1) - kGridDiv;
-                        const int rz = cz + lane / (2 * kGridDiv + 1) - kGridDiv;
-                        const float y0 = ry == 0 ? -FLT_MAX : gy + ry * edge - kRowMargin;
-                        const float y1 = ry == ny - 1 ? FLT_MAX : gy + (ry + 1) * edge + kRowMargin;
-                        const float z0 = rz == 0 ? -FLT_MAX : gz + rz * edge - kRowMargin;
-                        const float z1 = rz == nz - 1 ? FLT_MAX : gz + (rz + 1) * edge + kRowMargin;
-                        const float dy = fmaxf(0.0f, fmaxf(y0 - pi.y, pi.y - y1));
-                        const float dz = fmaxf(0.0f, fmaxf(z0 - pi.z, pi.z - z1));
-                        const float d2 = dy * dy + dz * dz;
-                        if (d2 < r2max)
-                        {
-                            const float hx = sqrtf(r2max - d2) * 1.0001f + kRowMargin;
-                            const float xa = pi.x - hx, xb = pi.x + hx;
-                            int a = 0, b = len;
-                            while (a < b)
-                            {
-                                const int m = (a + b) >> 1;
-                                if (sh_pos[o + m].x < xa)
-                                    a = m + 1;
-                                else
-                                    b = m;
-                            }
-                            int u = a, v = len;
-                            while (u < v)
-                            {
-                                const int m = (u + v) >> 1;
-                                if (sh_pos[o + m].x <= xb)
-                                    u = m + 1;
-                                else
-                                    v = m;
-                            }
-                            lo_r = o + a;
-                            cnt_r = u - a;
-                        }
-                    }
-                }
-                for (int r = 0; r < kRuns; ++r)
-                {
-                    const int lo = __shfl_sync(0xffffffffu, lo_r, r);
-                    const int cn = __shfl_sync(0xffffffffu, cnt_r, r);
-                    for (int jb = 0; jb < cn; jb += 32)
-                    {
-                        const bool jv = jb + lane < cn;
-                        const int qc = lo + (jv ? jb + lane : cn - 1);
-                        window(sh_slot[qc], jv, sh_pos[qc], sh_flag[qc]);
-                    }
-                }
+                sh_row[t][0] = j0;
+                sh_row[t][1] = j1;
             }
             else
-                for (int r = 0; r < kRuns; ++r)
+            {
+                const int u = t - kRows;
+                const int y = gy0 + u % kG, z = gz0 + u / kG;
+                if (y < ny && z < nz)
                 {
-                    const int j0 = sh_run[r][0], j1 = sh_run[r][1];
-                    for (int jb = j0; jb < j1; jb += 32)
+                    const int base = (z * ny + y) * nx;
+                    j0 = p.cell_start[base + gx0];
+                    j1 = p.cell_start[base + hxb + 1];
+                }
+                sh_home[u][0] = j0;
+                sh_home[u][1] = j1;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            int tot = 0, nh = 0, lo = INT_MAX, hi = INT_MIN, hmin = INT_MAX, hmax = INT_MIN;
+            for (int u = 0; u < kG * kG; ++u)
+            {
+                sh_home[u][2] = nh;
+                const int len = sh_home[u][1] - sh_home[u][0];
+                nh += len;
+                if (len > 0)
+                {
+                    hmin = min(hmin, sh_home[u][0]);
+                    hmax = max(hmax, sh_home[u][1]);
+                }
+            }
+            for (int r = 0; r < kRows; ++r)
+            {
+                sh_row[r][2] = tot;
+                const int len = sh_row[r][1] - sh_row[r][0];
+                tot += len;
+                if (len > 0)
+                {
+                    lo = min(lo, sh_row[r][0]);
+                    hi = max(hi, sh_row[r][1]);
+                }
+            }
+            n_home = nh;
+            n_stage = tot;
+            staged = tot <= kPlStage;
+            // every candidate offset of this group fits 16 bits, or the list goes 32-bit
+            if (PL16 && nh > 0 && (hi - 1 - hmin > 32767 || lo - (hmax - 1) < -32768))
+                atomicOr(&ctl->status, ST_WIDE);
+        }
+        __syncthreads();
+        const int nh = n_home;
+        if (nh == 0)
+            continue;
+        // the candidates of the group's rows are read by every warp of the block: stage them,
+        // kStageUnroll loads in flight per thread
+        if (staged)
+            for (int k0 = threadIdx.x; k0 < n_stage; k0 += kStageUnroll * blockDim.x)
+            {
+                float4 v[kStageUnroll];
+                unsigned int f[kStageUnroll];
+                int sl[kStageUnroll];
+#pragma unroll
+                for (int u = 0; u < kStageUnroll; ++u)
+                {
+                    const int k = k0 + u * static_cast<int>(blockDim.x);
+                    sl[u] = -1;
+                    if (k < n_stage)
                     {
-                        const int j = jb + lane;
-                        const bool jv = j < j1;
-                        const int jc = jv ? j : j1 - 1;
-                        window(jc, jv, pos[jc], need_fj ? fl[jc] : 0u);
+                        int a = 0, b = kRows - 1; // the last row whose offset is <= k
+                        while (a < b)
+                        {
+                            const int m = (a + b + 1) >> 1;
+                            if (sh_row[m][2] <= k)
+                                a = m;
+                            else
+                                b = m - 1;
+                        }
+                        sl[u] = sh_row[a][0] + (k - sh_row[a][2]);
+                        v[u] = pos[sl[u]];
+                        f[u] = fl[sl[u]];
                     }
                 }
-        }
-        if (lane == 0)
-        {
-            const int cnts[kLists] = {cnt0, cnt1, cnt2, cnt3};
 #pragma unroll
-            for (int q = 0; q < kLists; ++q)
+                for (int u = 0; u < kStageUnroll; ++u)
+                    if (sl[u] >= 0)
+                    {
+                        const int k = k0 + u * static_cast<int>(blockDim.x);
+                        sh_pos[k] = v[u];
+                        sh_slot[k] = sl[u];
+                        sh_flag[k] = static_cast<unsigned char>(f[u]);
+                    }
+            }
+        __syncthreads();
+        for (int hh = wid; hh < nh; hh += kPlWarps)
+        {
+            int hu = 0;
+            while (hu + 1 < kG * kG && sh_home[hu + 1][2] <= hh)
+                ++hu;
+            const int i = sh_home[hu][0] + (hh - sh_home[hu][2]);
+            const int hy = hu % kG, hz = hu / kG; // the home's cell in the group (y, z)
+            const unsigned int fi = fl[i];
+            const bool dyn = !(fi & PF_STATIC);
+            const bool on0 = dyn && l0;
+            const bool on1 = dyn && l1 && ((fi & PF_CHARGED) || p.coul_all);
+            const bool on2 = dyn && l2 && (fi & PF_HYDROPHOBIC);
+            const bool need_fj = l3 || on1 || on2;
+            float r2max = on0 ? r2_0 : 0.0f;
+            if (on1)
+                r2max = fmaxf(r2max, r2_1);
+            if (on2)
+                r2max = fmaxf(r2max, r2_2);
+            int cnt0 = 0, cnt1 = 0, cnt2 = 0, cnt3 = 0;
+            if (on0 || on1 || on2)
             {
-                int k = cnts[q];
-                if (k > p.pl[q].cap)
+                const float4 pi = pos[i];
+                // spring partners of i in registers: lane m holds partners m and m + 32 (slots, -1
+                // for none); a home with more than 64 compares every candidate with its ELL row
+                const int deg = p.spring_on ? p.se_deg[i] : 0;
+                const bool small = deg <= 64;
+                const int ps0 = small && lane < deg
+                                    ? static_cast<int>(p.se_col[static_cast<size_t>(lane) * stride + i] & kSlotMask)
+                                    : -1;
+                const int ps1 = small && lane + 32 < deg
+                                    ? static_cast<int>(p.se_col[static_cast<size_t>(lane + 32) * stride + i] & kSlotMask)
+                                    : -1;
+                // the lanes whose candidate is a spring partner: partner positions t in [0, 32)
+                // relative to the window's first candidate, OR-ed over the warp
+                auto partner_mask = [&](const int t0, const int t1) {
+                    unsigned int b = t0 >= 0 && t0 < 32 ? 1u << t0 : 0u;
+                    if (t1 >= 0 && t1 < 32)
+                        b |= 1u << t1;
+                    return __reduce_or_sync(0xffffffffu, b);
+                };
+                short *row0s = reinterpret_cast<short *>(p.pl[0].idx) + static_cast<size_t>(i) * cap0;
+                unsigned int *row0 = p.pl[0].idx + static_cast<size_t>(i) * cap0;
+                unsigned int *row1 = p.pl[1].idx + static_cast<size_t>(i) * cap1;
+                unsigned int *row2 = p.pl[2].idx + static_cast<size_t>(i) * cap2;
+                unsigned int *row3 = p.pl[3].idx + static_cast<size_t>(i) * cap3;
+                // One window of up to 32 candidates, one per lane; bonded marks the lanes whose
+                // candidate is a spring partner.
+                auto window = [&](const int j, const bool jv, const float4 pj, const unsigned int fj,
+                                  const unsigned int bonded) {
+                    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    bool in = jv && r2 < r2max && j != i && !((bonded >> lane) & 1u);
+                    if (!small)
+                        for (int k = 0; k < deg; ++k)
+                            in = in && static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask) != j;
+                    const bool st = (fj & PF_STATIC) != 0;
+                    if (on0)
+                    {
+                        const bool a0 = in && !st && r2 < r2_0;
+                        const unsigned int m0 = __ballot_sync(0xffffffffu, a0);
+                        if (a0)
+                        {
+                            const int at = cnt0 + __popc(m0 & below);
+                            if (at < cap0)
+                            {
+                                if (PL16)
+                                    row0s[at] = static_cast<short>(j - i);
+                                else
+                                    row0[at] = static_cast<unsigned int>(j);
+                            }
+                        }
+                        cnt0 += __popc(m0);
+                        if (l3)
+                        {
+                            const bool a3 = in && st && r2 < r2_0;
+                            const unsigned int m3 = __ballot_sync(0xffffffffu, a3);
+                            if (a3 && cnt3 + __popc(m3 & below) < cap3)
+                                row3[cnt3 + __popc(m3 & below)] = static_cast<unsigned int>(j) | kEntryStatic;
+                            cnt3 += __popc(m3);
+                        }
+                    }
+                    if (on1)
+                    {
+                        const bool a1 = in && ((fj & PF_CHARGED) || p.coul_all) && r2 < r2_1;
+                        const unsigned int m1 = __ballot_sync(0xffffffffu, a1);
+                        if (a1 && cnt1 + __popc(m1 & below) < cap1)
+                            row1[cnt1 + __popc(m1 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
+                        cnt1 += __popc(m1);
+                    }
+                    if (on2)
+                    {
+                        const bool a2 = in && (fj & PF_HYDROPHOBIC) && r2 < r2_2;
+                        const unsigned int m2 = __ballot_sync(0xffffffffu, a2);
+                        if (a2 && cnt2 + __popc(m2 & below) < cap2)
+                            row2[cnt2 + __popc(m2 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
+                        cnt2 += __popc(m2);
+                    }
+                };
+                if (staged)
                 {
-                    atomicOr(&ctl->status, ST_PAIR_CAPACITY);
-                    atomicMax(&ctl->max_row[q], k);
-                    k = p.pl[q].cap;
+                    // lane r bounds the home's run r (cell offsets -kD + r % kSpan in y and
+                    // -kD + r / kSpan in z; cell bounds widened by kRowMargin, the grid's outer
+                    // cells unbounded) by binary search. Every candidate inside the bounds is still
+                    // tested exactly; those outside are farther than the radius.
+                    int lo_r = 0, cnt_r = 0;
+                    if (lane < kRuns)
+                    {
+                        const int a = lane % kSpan, b = lane / kSpan;
+                        const int row = (hz + b) * kRowsD + (hy + a);
+                        const int len = sh_row[row][1] - sh_row[row][0], o = sh_row[row][2];
+                        if (len > 0)
+                        {
+                            const int ry = gy0 + hy + a - kD, rz = gz0 + hz + b - kD;
+                            const float y0 = ry == 0 ? -FLT_MAX : gy + ry * edge - kRowMargin;
+                            const float y1 = ry == ny - 1 ? FLT_MAX : gy + (ry + 1) * edge + kRowMargin;
+                            const float z0 = rz == 0 ? -FLT_MAX : gz + rz * edge - kRowMargin;
+                            const float z1 = rz == nz - 1 ? FLT_MAX : gz + (rz + 1) * edge + kRowMargin;
+                            const float dy = fmaxf(0.0f, fmaxf(y0 - pi.y, pi.y - y1));
+                            const float dz = fmaxf(0.0f, fmaxf(z0 - pi.z, pi.z - z1));
+                            const float d2 = dy * dy + dz * dz;
+                            if (d2 < r2max)
+                            {
+                                const float hx = sqrtf(r2max - d2) * 1.0001f + kRowMargin;
+                                const float xa_ = pi.x - hx, xb_ = pi.x + hx;
+                                int u0 = 0, v0 = len;
+                                while (u0 < v0)
+                                {
+                                    const int m = (u0 + v0) >> 1;
+                                    if (sh_pos[o + m].x < xa_)
+                                        u0 = m + 1;
+                                    else
+                                        v0 = m;
+                                }
+                                int u1 = u0, v1 = len;
+                                while (u1 < v1)
+                                {
+                                    const int m = (u1 + v1) >> 1;
+                                    if (sh_pos[o + m].x <= xb_)
+                                        u1 = m + 1;
+                                    else
+                                        v1 = m;
+                                }
+                                lo_r = o + u0;
+                                cnt_r = u1 - u0;
+                            }
+                        }
+                    }
+#if BS_PL_PACK
+                    // The bounded runs, empty ones dropped, are walked as one sequence of
+                    // candidates (k = 0 .. total-1, in run order, hence ascending slots) so that
+                    // every window but the last is full. Lane c holds the c-th non-empty run: its
+                    // first stage index and its first k; a lane finds the run of its k from the run
+                    // starts inside its window.
+                    const unsigned int ne = __ballot_sync(0xffffffffu, cnt_r > 0);
+                    int incl = cnt_r;
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1)
+                    {
+                        const int v = __shfl_up_sync(0xffffffffu, incl, d);
+                        if (lane >= d)
+                            incl += v;
+                    }
+                    const int total = __shfl_sync(0xffffffffu, incl, 31);
+                    const int nr = __popc(ne);
+                    int *cr = sh_cr[wid];
+                    if (cnt_r > 0)
+                    {
+                        const int c = __popc(ne & below);
+                        cr[2 * c] = lo_r;
+                        cr[2 * c + 1] = incl - cnt_r;
+                    }
+                    __syncwarp();
+                    const int lo_c = lane < nr ? cr[2 * lane] : 0;
+                    const int pre_c = lane < nr ? cr[2 * lane + 1] : total;
+                    const int nxt = __shfl_down_sync(0xffffffffu, pre_c, 1);
+                    const int end_c = lane + 1 < nr ? nxt : total;
+                    // each spring partner's index in the candidate sequence (-1: not a candidate):
+                    // the last run whose first slot is <= the partner's, by a binary search over
+                    // the lanes' runs; runs are contiguous slot ranges
+                    int pk0 = -1, pk1 = -1;
+                    if (deg > 0 && small && total > 0)
+                    {
+                        const int s_c = lane < nr ? sh_slot[lo_c] : INT_MAX;
+                        const int n_c = end_c - pre_c;
+                        auto locate = [&](const int ps) {
+                            int at = 0;
+#pragma unroll
+                            for (int step = 16; step > 0; step >>= 1)
+                            {
+                                const int v = __shfl_sync(0xffffffffu, s_c, (at + step) & 31);
+                                if (at + step < nr && v <= ps)
+                                    at += step;
+                            }
+                            const int s0 = __shfl_sync(0xffffffffu, s_c, at);
+                            const int n0 = __shfl_sync(0xffffffffu, n_c, at);
+                            const int k0 = __shfl_sync(0xffffffffu, pre_c, at);
+                            return ps >= s0 && ps < s0 + n0 ? k0 + (ps - s0) : -1;
+                        };
+                        pk0 = locate(ps0);
+                        if (deg > 32)
+                            pk1 = locate(ps1);
+                    }
+                    for (int wb = 0; wb < total; wb += 32)
+                    {
+                        const int k = wb + lane;
+                        const int r0 = __popc(__ballot_sync(0xffffffffu, lane < nr && end_c <= wb));
+                        const int t = pre_c - wb;
+                        const unsigned int starts =
+                            __reduce_or_sync(0xffffffffu, (lane < nr && t > 0 && t < 32) ? (1u << t) : 0u);
+                        const int rk = min(r0 + __popc(starts & ((2u << lane) - 1u)), nr - 1);
+                        const int lo = __shfl_sync(0xffffffffu, lo_c, rk);
+                        const int pre = __shfl_sync(0xffffffffu, pre_c, rk);
+                        const bool jv = k < total;
+                        const int qc = jv ? lo + (k - pre) : lo;
+                        const unsigned int bonded =
+                            deg > 0 && small ? partner_mask(pk0 < 0 ? -1 : pk0 - wb, pk1 < 0 ? -1 : pk1 - wb) : 0u;
+                        window(sh_slot[qc], jv, sh_pos[qc], sh_flag[qc], bonded);
+                    }
+#else
+                    for (int r = 0; r < kRuns; ++r)
+                    {
+                        const int lo = __shfl_sync(0xffffffffu, lo_r, r);
+                        const int cn = __shfl_sync(0xffffffffu, cnt_r, r);
+                        for (int jb = 0; jb < cn; jb += 32)
+                        {
+                            const bool jv = jb + lane < cn;
+                            const int qc = lo + (jv ? jb + lane : cn - 1);
+                            const int j0 = __shfl_sync(0xffffffffu, sh_slot[qc], 0);
+                            const unsigned int bonded =
+                                deg > 0 && small ? partner_mask(ps0 < 0 ? -1 : ps0 - j0, ps1 < 0 ? -1 : ps1 - j0) : 0u;
+                            window(sh_slot[qc], jv, sh_pos[qc], sh_flag[qc], bonded & (jv ? ~0u : 0u));
+                        }
+                    }
+#endif
                 }
-                p.pl[q].cnt[i] = k;
+                else
+                    for (int r = 0; r < kRuns; ++r)
+                    {
+                        const int row = (hz + r / kSpan) * kRowsD + (hy + r % kSpan);
+                        const int j0 = sh_row[row][0], j1 = sh_row[row][1];
+                        for (int jb = j0; jb < j1; jb += 32)
+                        {
+                            const int j = jb + lane;
+                            const bool jv = j < j1;
+                            const int jc = jv ? j : j1 - 1;
+                            const unsigned int bonded =
+                                deg > 0 && small ? partner_mask(ps0 < 0 ? -1 : ps0 - jb, ps1 < 0 ? -1 : ps1 - jb) : 0u;
+                            window(jc, jv, pos[jc], need_fj ? fl[jc] : 0u, bonded);
+                        }
+                    }
+            }
+            if (lane == 0)
+            {
+                const int cnts[kLists] = {cnt0, cnt1, cnt2, cnt3};
+#pragma unroll
+                for (int q = 0; q < kLists; ++q)
+                {
+                    int k = cnts[q];
+                    if (k > p.pl[q].cap)
+                    {
+                        atomicOr(&ctl->status, ST_PAIR_CAPACITY);
+                        atomicMax(&ctl->max_row[q], k);
+                        k = p.pl[q].cap;
+                    }
+                    p.pl[q].cnt[i] = k;
+                }
             }
         }
     }
@@ -1099,9 +1242,9 @@ int launch_rebuild(const Params &p, cudaStream_t st)
     launched += 4;
     if (p.nsys > 0 || p.pl_sparse)
         return launched + launch_batch_pairlist(p, st);
-    // one block per cell of the grid (its size is only known on the device: cover the capacity;
-    // blocks past the last cell return at once)
-    const int plb = p.cell_cap;
+    // one block per group of kGridDiv^3 cells (the grid's size is only known on the device: cover
+    // the capacity; blocks past the last group return at once, and the kernel strides over groups)
+    const int plb = p.cell_cap / (kGridDiv * kGridDiv * kGridDiv) + 1;
     if (p.pl16)
         launch_chain(k_pairlist<true>, plb, kPlWarps * 32, 0, st, p);
     else

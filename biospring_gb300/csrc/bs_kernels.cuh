@@ -38,8 +38,15 @@ constexpr int kRebuildBlocking = ST_NONFINITE | ST_PAIR_CAPACITY | ST_CELL_CAPAC
 #ifndef BS_PDL_STEP
 #define BS_PDL_STEP 0
 #endif
+// Cell-block list build on cells of half the list radius, in groups of 2 x 2 x 2 cells per block,
+// the bounded runs packed into full windows and spring partners excluded by lane masks: 323
+// candidates tested per particle instead of 505 at 100k (rebuild 355 -> 310 us).
 #ifndef BS_GRID_DIV
-#define BS_GRID_DIV 1
+#define BS_GRID_DIV 2
+#endif
+// the cell-block list build walks the bounded runs as one packed sequence when there are many
+#ifndef BS_PL_PACK
+#define BS_PL_PACK (BS_GRID_DIV > 1)
 #endif
 #ifndef BS_PL_WARPS
 #define BS_PL_WARPS 8
@@ -47,9 +54,11 @@ constexpr int kRebuildBlocking = ST_NONFINITE | ST_PAIR_CAPACITY | ST_CELL_CAPAC
 #ifndef BS_PL_STAGE
 #define BS_PL_STAGE 2048
 #endif
-constexpr int kGridDiv = BS_GRID_DIV; // search-grid cells per list radius (stencil of +-kGridDiv cells)
+constexpr int kGridDiv = BS_GRID_DIV; // cell-block list build: cells per list radius (stencil of +-kGridDiv cells)
+constexpr int kSparseDiv = 1;         // warp-per-particle list build (sparse systems, batches): cells of the radius
 constexpr int kPlWarps = BS_PL_WARPS; // warps per block (one cell) in the pair-list build
 constexpr int kPlStage = BS_PL_STAGE; // candidate positions staged in shared memory per block
+constexpr int kPlMinBlocks = 4;       // resident list-build blocks per SM (the stage allows 4)
 constexpr int kPlBatch = 16;         // home particles per warp
 constexpr int kPlBatchesPerCell = 4; // warps per cell (a cell with more than 64 particles loops)
 constexpr int kPlMaxDeg = 48;        // spring partners kept in shared memory per home particle

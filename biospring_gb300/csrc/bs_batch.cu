@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 2) k_batch_run(Params p, int c
             for (int g0 = 0; g0 < span; g0 += stride)
             {
                 const int g = g0 + me;
-                pend |= particle_step<MODE_STEP, SM, T>(p, n0 + g / T, g % T, n1, sb, lb, false, e);
+                pend |= particle_step<MODE_STEP, SM, T, false>(p, n0 + g / T, g % T, n1, sb, lb, false, e);
             }
             if (pend)
             {

@@ -920,6 +920,8 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
             return fail(s, BS_E_ARG, "rigid bodies are not available for batched ensembles");
         if (c.probe_enable)
             return fail(s, BS_E_ARG, "the probe is not available for batched ensembles");
+        if (c.potentialgrid_enable || c.densitygrid_enable)
+            return fail(s, BS_E_ARG, "field grids are not available for batched ensembles");
         std::vector<int> sys_of_id(s->n);
         max_sys = 0;
         for (size_t b = 0; b + 1 < s->sys_off.size(); ++b)

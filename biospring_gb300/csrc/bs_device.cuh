@@ -648,8 +648,11 @@ template <int T> __device__ __forceinline__ float group_sum(float v)
 // terms and integrates (reading buffer sb, writing sb ^ 1). Slots at or beyond `send` are
 // inactive. Every lane of the warp must call it (shuffles). Adds the particle's energies to
 // eacc (spring, steric, Coulomb, hydrophobic, IMPALA, kinetic) and returns the status bits it
-// raised (ST_NONFINITE, ST_STALE).
-template <int MODE, int SM, int T>
+// raised (ST_NONFINITE, ST_STALE). SINGLE selects the single-system form: field-grid forces and
+// Coulomb rows walked by the whole warp. The batched kernel leaves both out (fewer live registers
+// under its 64-register budget: with them its spills grew and its step slowed by 7%); it walks
+// Coulomb rows with the particle's own lanes (the same pairs, summed in another order).
+template <int MODE, int SM, int T, bool SINGLE = true>
 __device__ __forceinline__ int particle_step(const Params &p, const int s, const int t, const int send,
                                              const int sb, const int lb, const bool ext_on, float (&eacc)[6])
 {
@@ -696,8 +699,7 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             fz = fmaf(sz, kf, fz);
             e[1] = es * p.steric_scale;
         }
-#if !BS_COUL_WARP
-        if (p.coulomb_on && (fi & PF_CHARGED))
+        if ((!SINGLE || !BS_COUL_WARP) && p.coulomb_on && (fi & PF_CHARGED))
         {
             float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
             coulomb_forces<T>(p, s, t, pi, p.chg[lb][s], pos, p.chg[lb], sx, sy, sz, es);
@@ -706,7 +708,6 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             fz = fmaf(sz, p.k_elec_f, fz);
             e[2] = es * p.k_elec_e;
         }
-#endif
         if (p.hydro_on && (fi & PF_HYDROPHOBIC))
         {
             float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
@@ -734,11 +735,10 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
                 e[k] = 0.f;
         }
     }
-#if BS_COUL_WARP
     // Coulomb pairs, a warp at a time: few particles are charged, so instead of a particle's own
     // T lanes, all 32 lanes of the warp walk the row of each charged particle of the warp in turn
     // (coalesced entries, one or two per lane), and the lead lane of that particle takes the sum.
-    if (p.coulomb_on)
+    if (SINGLE && BS_COUL_WARP && p.coulomb_on)
     {
         const int lane = static_cast<int>(threadIdx.x & 31);
         unsigned todo = __ballot_sync(0xffffffffu, lead && active && (fi & PF_CHARGED));
@@ -764,7 +764,6 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             }
         }
     }
-#endif
     if (lead && s < send)
     {
         if (!active)
@@ -785,7 +784,7 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
         {
             const float4 v = p.vel[sb][s];
             // ---- field grids (SpringNetwork.cpp:110-118) ----
-            if (p.fg_on[0] || p.fg_on[1])
+            if (SINGLE && (p.fg_on[0] || p.fg_on[1]))
                 field_forces(p, pi, p.chg[lb][s], p.fg_on[1] ? p.bur[lb][s] : 0.0f, fx, fy, fz, e[2]);
             // ---- viscosity (Particle.cpp:80-84) ----
             if (p.visc_on)

@@ -351,7 +351,7 @@ int bs_adjoint(bs_sim *sim, int32_t nsteps, int32_t checkpoint, const float *tar
  * thread-block cluster owns whole systems; bs_get_positions / bs_get_velocities /
  * bs_compute_forces work on the concatenation, bs_get_energies gives the sums over systems and
  * bs_get_system_energies each system's. External forces and the pair/cell diagnostics are for
- * single systems (BS_E_STATE). */
+ * single systems (BS_E_STATE); rigid bodies, the probe and field grids are BS_E_ARG at bs_setup. */
 int bs_set_systems(bs_sim *sim, int32_t nsys, const int64_t *offsets);
 
 /* Energies of every system of a batch after its last step: double[nsys * BS_NUM_ENERGIES]. */

@@ -156,3 +156,11 @@ def test_batch_rejections(ensemble):
     with pytest.raises(BsError, match="two systems"):
         bad.setup(ensemble.bs_config())
     bad.close()
+    grid = SpringNetwork()
+    grid.addParticles(ensemble.xyz[:400])
+    grid.setSystems([0, 200, 400])
+    cfg = ensemble.bs_config()
+    cfg.densitygrid_enable = 1
+    with pytest.raises(BsError, match="field grids"):
+        grid.setup(cfg)
+    grid.close()

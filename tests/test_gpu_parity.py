@@ -211,6 +211,42 @@ def test_charges_after_setup():
     orc.close()
 
 
+def test_dense_neighbourhood_beyond_stage():
+    """A jittered 2.5 A lattice (0.064 particles per A^3, 8,000 particles): a block's group of
+    half-radius cells has about 3,400 candidates within reach of a 12.5 A list radius, more than the
+    2,048 staged in shared memory, so the list build reads the rows from global memory (with the
+    spring partners excluded by slot offsets). Steric and Coulomb pair sets bit-exact against the
+    oracle (decoded from the lists), forces within the force bar."""
+    from biospring_gb300 import capi
+    from biospring_gb300 import workloads as W
+    rng = np.random.default_rng(17)
+    g = np.arange(20, dtype=np.float32) * 2.5
+    xyz = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    xyz = (xyz + rng.uniform(-0.3, 0.3, xyz.shape)).astype(np.float32)
+    n = xyz.shape[0]
+    ij = W.pairs_within(xyz, 2.6)
+    r0 = np.linalg.norm(xyz[ij[:, 0]] - xyz[ij[:, 1]], axis=1).astype(np.float32)
+    charge = np.where(rng.random(n) < 0.2, rng.choice([-1.0, 1.0], n), 0.0).astype(np.float32)
+    cfg = dict(timestep=0.01, spring_enable=1, steric_enable=1, steric_cutoff=12.0,
+               steric_mode=capi.BS_STERIC_LINEAR, coulomb_enable=1, coulomb_cutoff=12.0, coulomb_dielectric=4.0,
+               dielectric_mode=0, rebuild_every=10, list_skin=0.5)
+    s = W.System("lattice2.5", xyz, ij, r0, np.ones(ij.shape[0], np.float32), cfg, charge=charge,
+                 radius=np.full(n, 1.0, np.float32), epsilon=np.full(n, 0.5, np.float32))
+    net = gpu_network(s)
+    net.computeForces()
+    orc = po.Oracle(s)
+    orc.compute_forces()
+    for term in (0, 1):
+        np.testing.assert_array_equal(net.getPairs(term), orc.pairs(term).astype(np.int64))
+    fo = orc.forces()
+    tol, own = force_tolerance(s, fo)
+    err = rel_l2(net.getForces(), fo, dynamic_mask(s))
+    print(f"lattice: {ij.shape[0]} springs, {net.getPairs(0).shape[0]} steric pairs, force rel err {err:.2e}")
+    assert err <= tol
+    net.close()
+    orc.close()
+
+
 def test_long_trajectory_tracks_oracle():
     """2,000-particle Calpha network, 200 damped steps (the plain CPU/GPU configuration)."""
     from biospring_gb300 import workloads as W

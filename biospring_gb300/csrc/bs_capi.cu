@@ -998,6 +998,11 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     for (int64_t i = 0; i < n; ++i)
         maxdeg = std::max(maxdeg, deg[i]);
     p.sp_maxdeg = maxdeg;
+    // Spring-table rebuild: kBuildLanes threads per slot overlap a slot's partner lookups, but
+    // their column-major stores do not coalesce, which only L2 absorbs; a table well beyond L2
+    // (large batches) is rebuilt one thread per slot, with each column stored contiguously.
+    const double ell_bytes = static_cast<double>(npad) * maxdeg * 12.0;
+    p.ell_lanes = ell_bytes > 48.0e6 ? 1 : kBuildLanes;
 
     // ---- per-particle packed parameters ----
     // Steric factors: eps_ij r_ij^m = (a_i b_i^m)(a_j b_j^m) with eps_ij = a_i a_j, r_ij = b_i b_j

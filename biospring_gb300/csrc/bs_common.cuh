@@ -173,6 +173,7 @@ struct Params
     const float *sp_k;
     const float *sp_r0;
     int sp_maxdeg;
+    int ell_lanes;            // threads per slot of the spring-table rebuild (1 or kBuildLanes)
     // springs: sorted-space ELL, column-major [k * npad + slot], each row ascending by partner slot
     unsigned int *se_col;
     float *se_k;

@@ -386,9 +386,10 @@ __global__ void __launch_bounds__(kBuildBlock) k_reorder(Params p)
     }
 }
 
-// Springs of every slot in the new layout, partners as slots (ELL, column-major). kBuildLanes
-// consecutive threads share a slot and take every kBuildLanes-th spring of its caller-order row,
-// so the row is read with contiguous loads and the partner lookups of a slot overlap.
+// Springs of every slot in the new layout, partners as slots (ELL, column-major). ell_lanes
+// consecutive threads share a slot and take every ell_lanes-th spring of its caller-order row,
+// so the row is read with contiguous loads and the partner lookups of a slot overlap; with one
+// lane per slot, the threads of a warp store each column contiguously.
 __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
 {
     pdl_enter();
@@ -396,7 +397,8 @@ __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
     if (status_of(ctl) & kRebuildBlocking)
         return;
     const long long g = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int s = static_cast<int>(g / kBuildLanes), t = static_cast<int>(g % kBuildLanes);
+    const int L = p.ell_lanes;
+    const int s = static_cast<int>(g / L), t = static_cast<int>(g % L);
     if (s >= p.npad)
         return;
     if (s >= p.n)
@@ -408,7 +410,7 @@ __global__ void __launch_bounds__(kBuildBlock) k_spring_ell(Params p)
     const int id = p.perm[ctl->lbuf][s];
     const int r0 = p.sp_row[id], r1 = p.sp_row[id + 1];
     const size_t stride = static_cast<size_t>(p.npad);
-    for (int e = r0 + t; e < r1; e += kBuildLanes)
+    for (int e = r0 + t; e < r1; e += L)
     {
         const unsigned int c = p.sp_col[e];
         const unsigned int slot = static_cast<unsigned int>(p.inv[c & kSlotMask]);
@@ -1237,7 +1239,7 @@ int launch_rebuild(const Params &p, cudaStream_t st)
     launch_chain(k_cell_sort, 1216, kBuildBlock, 0, st, p);
     launch_chain(k_reorder, nb, kBuildBlock, 0, st, p);
     launch_chain(k_spring_ell,
-                 static_cast<unsigned>((static_cast<long long>(p.npad) * kBuildLanes + kBuildBlock - 1) / kBuildBlock),
+                 static_cast<unsigned>((static_cast<long long>(p.npad) * p.ell_lanes + kBuildBlock - 1) / kBuildBlock),
                  kBuildBlock, 0, st, p);
     launched += 4;
     if (p.nsys > 0 || p.pl_sparse)

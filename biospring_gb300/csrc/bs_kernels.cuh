@@ -18,7 +18,7 @@ constexpr int kStepBlock = 128; // adjoint and diagnostic kernels
 constexpr int kStepKernelBlock = BS_STEP_BLOCK;
 constexpr int kStepMinBlocks = BS_STEP_MIN_BLOCKS;
 constexpr int kBuildBlock = 128;
-constexpr int kBuildLanes = 8;    // lanes sharing one particle in the pair-list build
+constexpr int kBuildLanes = 8;    // threads per slot of the spring-table rebuild when the table fits L2
 constexpr int kBboxBlock = 256;
 constexpr int kMaxEnergyBlocks = 1 << 16;
 

@@ -1,9 +1,9 @@
 """Pins the CPU oracle (oracle/bs_oracle.cpp) to the reference's own outputs.
 
 The golden fixtures were produced by the compiled reference (tests/golden/make_golden.py).
-On the machine that generated them the oracle must reproduce them bit for bit; elsewhere a
-different libm may move the last bit of exp/pow, so the comparisons fall back to 1e-6
-relative there (the flag is the fixture generator's host, recorded in the design doc).
+On the machine that generated them (x86-64, where the reference itself can be compiled) the
+oracle must reproduce them bit for bit; elsewhere a different libm may move the last bit of
+exp/pow, so the comparisons fall back to 1e-6 relative there.
 """
 
 import os

@@ -207,6 +207,12 @@ def test_charges_after_setup():
     net.computeStep(3)
     orc.step(3)
     assert np.abs(net.getPositions() - orc.positions()).max() < 1e-4
+    # rejected before anything changes: non-finite charges, a wrong count
+    from biospring_gb300 import BsError
+    with pytest.raises(BsError, match="finite"):
+        net.setCharges(np.full(s.n, np.nan, np.float32))
+    with pytest.raises(ValueError):
+        net.setCharges(q2[:-1])
     net.close()
     orc.close()
 

@@ -200,8 +200,8 @@ __global__ void __launch_bounds__(1024) k_batch_cell_scan(Params p)
 // partners of the steric term apart); the warp walks the (2 kSparseDiv + 1)^2 contiguous x-runs of
 // the neighbour cells, 32 candidates per pass, and a ballot appends the accepted ones to the row
 // in ascending slot order. Used for batched ensembles (BATCH: each system's own grid) and for
-// sparse single systems (a few particles per cell or fewer), where one block per cell would
-// mostly schedule empty blocks.
+// sparse single systems (a few particles per cell or fewer), where one block per group of cells
+// would mostly schedule empty blocks.
 template <bool PL16, bool BATCH>
 __global__ void __launch_bounds__(kBatchPlWarps * 32) k_batch_pairlist(Params p)
 {

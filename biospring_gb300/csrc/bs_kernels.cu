@@ -20,8 +20,8 @@
 // Rebuild (every K steps, or when a particle drifted more than skin/2):
 //   k_bbox -> k_cell_count -> k_cell_scan -> k_cell_place -> k_cell_sort -> k_reorder
 //   -> k_spring_ell -> k_pairlist
-// Step: k_step, one thread per particle, gathers its springs and nonbonded pairs (no atomics
-// on forces, so results are deterministic) and integrates in the same pass.
+// Step: k_step, T consecutive lanes per particle, gathers its springs and nonbonded pairs (no
+// atomics on forces, so results are deterministic) and integrates in the same pass.
 //
 // Reference behaviour reproduced (paths inside the BioSpring project):
 //   cell grid and cell id           src/nsearch.hpp:277-293, 342-390 (FP64, same formula; the

@@ -72,22 +72,29 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device: int = 0):
+    def __init__(self, device: int = 0, interval_ms: int = 50):
         self.device = device
+        self.interval_ms = interval_ms
         self.proc = None
         self.lines: list[str] = []
         self.thread = None
 
-    def start(self):
+    def start(self, wait_s: float = 5.0):
+        """Starts sampling and returns once the first sample has arrived (nvidia-smi takes a while
+        to start), so that the timed region that follows is sampled from its beginning."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.interval_ms)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, FileNotFoundError):
             self.proc = None
             return
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        t_end = time.perf_counter() + wait_s
+        while not self.lines and self.proc.poll() is None and time.perf_counter() < t_end:
+            time.sleep(0.01)
+        self.skip = len(self.lines)  # samples taken before the timed region are not counted
 
     def _read(self):
         for line in self.proc.stdout:
@@ -105,7 +112,9 @@ class ClockSampler:
             self.thread.join(timeout=2)
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        # the samples from the timed region on; the last one before it if none came during
+        lines = self.lines[getattr(self, "skip", 0):] or self.lines[-1:]
+        for line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -585,19 +594,21 @@ def run_reference(args) -> dict | None:
     os.environ["OMP_NUM_THREADS"] = str(cores)
     system = make_workload(seed=42)
     orc = pyoracle.Oracle(system)
-    for _ in range(args.warmup):
+    # a bounded sample: a 100k step takes about 0.2 s on 16 cores, so at most 200 timed steps
+    steps = min(args.steps, 200)
+    for _ in range(min(args.warmup, 5)):
         orc.time_steps(1)
-    t = orc.time_steps(args.steps)
+    t = orc.time_steps(steps)
     orc.close()
-    value = system.n * args.steps / t
+    value = system.n * steps / t
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3 / args.steps, "higher_is_better": True,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": t * 1e3 / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": "uniform_lj_100k (same system as the native arm)", "global_batch": system.n},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full steps after {args.warmup} warm-up steps, OpenMP on all cores"},
+                         "sample": f"{steps} full steps after {min(args.warmup, 5)} warm-up steps, OpenMP on all cores"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -605,7 +616,7 @@ def run_reference(args) -> dict | None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

@@ -213,7 +213,7 @@ def test_fit_harness_descends():
         opt.zero_grad()
         loss = SpringFitLoss.apply(k, r0, net, target, nsteps, 20)
         loss.backward()
-        losses.append(float(loss))
+        losses.append(float(loss.detach()))
         opt.step()
     print("fit losses", losses)
     assert all(b < a for a, b in zip(losses, losses[1:]))

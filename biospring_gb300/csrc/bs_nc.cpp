@@ -335,6 +335,19 @@ class NcReader
             if (nrecvars == 1)
                 recsize = per * ts;
         }
+        // the whole extent must lie in the file before anything is allocated: a damaged header
+        // can declare any size (the checks are written so that they cannot overflow)
+        const uint64_t size = buf_.size();
+        const bool fits =
+            nrec == 0 ||
+            (v.begin <= size && per <= (size - v.begin) / static_cast<uint64_t>(ts) &&
+             (nrec == 1 || (recsize > 0 && nrec - 1 <= (size - v.begin) / recsize &&
+                            per <= (size - v.begin - (nrec - 1) * recsize) / static_cast<uint64_t>(ts))));
+        if (!fits)
+        {
+            err = "array \"" + v.name + "\" lies past the end of the file";
+            return false;
+        }
         out.resize(per * nrec);
         for (uint64_t r = 0; r < nrec; ++r)
         {

@@ -159,3 +159,28 @@ def test_msp_grid_keys():
     assert c.potentialgrid_scale == 2.5 and c.densitygrid_scale == 0.25
     d = capi.default_config()
     assert d.potentialgrid_scale == 1.0 and d.densitygrid_scale == 1.0 and d.potentialgrid_path == b""
+
+
+def test_dx_reader_survives_truncation_and_corruption(tmp_path):
+    """An OpenDX map cut short anywhere, or with a character overwritten, is either read (and then
+    holds as many values as its header declares) or refused with an error code."""
+    src = str(tmp_path / "ok.dx")
+    g = np.random.default_rng(1).standard_normal((5, 4, 3)).astype(np.float32)
+    W.write_dx(src, g, np.array([1.0, 2.0, 3.0]), np.array([0.5, 0.5, 0.5]))
+    text = open(src, "rb").read()
+    rng = np.random.default_rng(2)
+    blobs = [text[:cut] for cut in range(0, len(text), 5)]
+    for _ in range(400):
+        b = bytearray(text)
+        b[int(rng.integers(0, len(b)))] = int(rng.choice(list(b"0123456789 -.e\nabxyz#")))
+        blobs.append(bytes(b))
+    path = str(tmp_path / "t.dx")
+    read = 0
+    for blob in blobs:
+        with open(path, "wb") as fh:
+            fh.write(blob)
+        rc, _, sc, _, _ = _read_dx(path)
+        if rc == capi.BS_OK:
+            read += 1
+            assert sc.size == int(np.prod(sc.shape))
+    assert 0 < read < len(blobs)

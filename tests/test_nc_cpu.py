@@ -161,3 +161,27 @@ def test_reference_example_topology():
     np.testing.assert_array_equal(t["is_static"], (v["dynamicstate"] == 0).astype(np.uint8))
     np.testing.assert_array_equal(t["sasa"], v["surfaceaccessibility"])
     assert t["hydrophobicity"] is None
+
+
+def test_truncated_and_corrupted_files_fail_cleanly(tmp_path):
+    """A topology cut short anywhere, or with a header byte overwritten, is either read or refused
+    with an error: the reader checks every size and offset against the file before it reads."""
+    src = str(tmp_path / "ok.nc")
+    write_topology(src)
+    data = open(src, "rb").read()
+    rng = np.random.default_rng(5)
+    blobs = [data[:cut] for cut in range(0, len(data), 7)]
+    for _ in range(400):
+        b = bytearray(data)
+        b[int(rng.integers(0, min(len(b), 400)))] = int(rng.integers(0, 256))
+        blobs.append(bytes(b))
+    path = str(tmp_path / "t.nc")
+    refused = 0
+    for blob in blobs:
+        with open(path, "wb") as fh:
+            fh.write(blob)
+        try:
+            capi.read_nc(path)
+        except BsError:
+            refused += 1
+    assert refused >= len(data) // 7  # every cut file is refused

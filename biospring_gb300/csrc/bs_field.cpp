@@ -75,6 +75,8 @@ bool read_dx(const char *path, int shape[3], double origin[3], double spacing[3]
     std::ifstream in(path);
     if (!in)
         return fail(err, std::string("cannot open '") + path + "'");
+    std::ifstream probe(path, std::ios::binary | std::ios::ate);
+    const double file_bytes = probe ? static_cast<double>(probe.tellg()) : -1.0;
     std::string line;
     // comment lines, then the grid counts
     do
@@ -106,13 +108,28 @@ bool read_dx(const char *path, int shape[3], double origin[3], double spacing[3]
             return fail(err, "cannot read scaling factors (found '" + line + "')");
         delta[r] = d[r]; // the diagonal
     }
+    // A damaged header may declare anything: the counts, the cell sizes and the number of values
+    // the file can hold (at least two characters each) are checked before any size is derived
+    // or allocated.
+    constexpr long kMaxCount = 1L << 24;
     for (int a = 0; a < 3; ++a)
     {
         if (counts[a] < 0)
             return fail(err, "cannot read grid dimensions (negative count)");
+        if (counts[a] > kMaxCount)
+            return fail(err, "cannot read grid dimensions (more than 16777216 points along an axis)");
+        if (!(delta[a] > 0.0f) || !std::isfinite(delta[a]) || !std::isfinite(o[a]))
+            return fail(err, "cannot read scaling factors (a finite cell size > 0 and a finite origin are "
+                             "required)");
         origin[a] = static_cast<double>(o[a]);
         spacing[a] = static_cast<double>(delta[a]);
     }
+    const double declared = static_cast<double>(counts[0]) * static_cast<double>(counts[1]) *
+                            static_cast<double>(counts[2]);
+    if (file_bytes >= 0.0 && declared > file_bytes / 2.0 + 1.0)
+        return fail(err, "cannot access grid data (the file is too short for the " + std::to_string(counts[0]) +
+                             " x " + std::to_string(counts[1]) + " x " + std::to_string(counts[2]) +
+                             " values declared)");
     field_shape(counts, origin, spacing, shape);
     if (!values)
         return true;

@@ -126,7 +126,13 @@ def test_library_dx_reader_errors(tmp_path):
         "delta.dx": text[:3] + ["delt 1 0 0"] + text[4:],
         "short.dx": text[:8],
         "tokens.dx": text[:8] + ["1 1 1 1"] + text[9:],
+        # refused from the header alone, before a size is derived or allocated
+        "huge.dx": ["object 1 class gridpositions counts 5000 4000 3000"] + text[2:],
+        "axis.dx": ["object 1 class gridpositions counts 1 1 20000000"] + text[2:],
+        "zero_delta.dx": text[:3] + ["delta 0 0 0"] + text[4:],
     }
+    reason = {"huge.dx": "too short for the 5000 x 4000 x 3000", "axis.dx": "more than 16777216",
+              "zero_delta.dx": "cell size > 0"}
     for name, lines in cases.items():
         path = tmp_path / name
         if lines is not None:
@@ -134,6 +140,7 @@ def test_library_dx_reader_errors(tmp_path):
         rc, msg, *_ = _read_dx(str(path))
         assert rc == capi.BS_E_ARG, name
         assert msg.startswith("OpenDXReader:"), (name, msg)
+        assert reason.get(name, "") in msg, (name, msg)
 
 
 @pytest.mark.skipif(not po.have_reference(), reason="the compiled reference is not present")

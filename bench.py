@@ -29,6 +29,7 @@ Prints one JSON line.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -52,8 +53,23 @@ SPRING_BYTES_PER_ENTRY = 12.0         # partner index + stiffness + rest length
 REBUILD_BYTES_PER_PARTICLE = 104.0    # key 4 + permutation 4 + gather/scatter of x, v, parameters 3 x 32
 CTL_BYTES = 288                       # device control block (status, step count, energies) read per bs_step
 # DRAM bytes (read + write) of one k_step launch on this workload after an L2 flush, from one ncu
-# capture (dram__bytes_read.sum + dram__bytes_write.sum; profiles/k_step_uniform_lj_100k.md)
-STEP_KERNEL_TRAFFIC_BYTES = 78.07e6 + 2.34e6
+# capture of dram__bytes_read.sum + dram__bytes_write.sum, and the digest of the step kernel's
+# sources that capture ran on: when the sources have changed since, the line marks the figure stale.
+STEP_KERNEL_TRAFFIC = {"bytes": 78.07e6 + 2.34e6, "sources_sha": "unrecorded", "captured": "2026-12-03"}
+STEP_KERNEL_SOURCES = ("biospring_gb300/csrc/bs_device.cuh", "biospring_gb300/csrc/bs_kernels.cu",
+                       "biospring_gb300/csrc/bs_kernels.cuh", "biospring_gb300/csrc/bs_common.cuh")
+DIELECTRIC_NOTE = ("Coulomb eps = 4r (distance-dependent), as the 100k configuration states; the reference's "
+                   "electrostatic.hpp has the constant form only, so this term follows the restatement's "
+                   "extension (E = K q q / (4 r^2)); the restatement is bit-exact with the reference in constant mode")
+
+
+def step_sources_sha() -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for rel in STEP_KERNEL_SOURCES:
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
 
 
 def peaks() -> dict:
@@ -146,10 +162,24 @@ def replica_throughput(n: int, steps: int, slowest_ms: float, world: int) -> flo
     return world * n * steps / (slowest_ms * 1e-3)
 
 
-def make_workload(seed: int = 42):
+def make_workload(seed: int = 42, dielectric_mode: int = 1):
     from biospring_gb300 import workloads as W
-    return W.uniform_lj(n=N_PARTICLES, box=BOX, seed=seed, dielectric_mode=1, rebuild_every=REBUILD,
+    return W.uniform_lj(n=N_PARTICLES, box=BOX, seed=seed, dielectric_mode=dielectric_mode, rebuild_every=REBUILD,
                         list_skin=0.5)
+
+
+def workload_config(system, world: int) -> dict:
+    """The `config` object of both arms' lines (identical for the same workload and N)."""
+    dbar = 2.0 * system.ij.shape[0] / system.n
+    return {
+        "workload": f"uniform_lj_100k: N={system.n}, cube {BOX:g} A, springs<5A (mean degree {dbar:.2f}), "
+                    f"20% charged, Coulomb eps=4r 12 A, LJ 12-6 Amber 12 A, rebuild every {REBUILD} steps, "
+                    "list skin 0.5 A",
+        "global_batch": system.n * world,
+        "parallelism": f"replicas{world}" if world > 1 else "single",
+        "dielectric": DIELECTRIC_NOTE,
+        "l2": "GPU arm: flushed (256 MB write) before every timed step; CPU arm: no flush (host caches)",
+    }
 
 
 def algorithmic(system, net) -> dict:
@@ -266,15 +296,9 @@ def run_native(args) -> dict:
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded uniform fill, springs, charges)",
-        "config": {
-            "workload": f"uniform_lj_100k: N={system.n}, cube {BOX:g} A, springs<5A (mean degree "
-                        f"{alg['mean_spring_degree']:.2f}), 20% charged, Coulomb eps=4r 12 A, LJ 12-6 Amber 12 A, "
-                        f"rebuild every {REBUILD} steps, list skin 0.5 A",
-            "global_batch": system.n * world,
-            "parallelism": f"replicas{world}" if world > 1 else "single",
-            "l2": "flushed (256 MB write) before every timed step",
-            "timing": "CUDA events on the library stream around each step (rebuild on every 10th)",
-        },
+        "config": workload_config(system, world),
+        "timing": "CUDA events on the library stream around each step (rebuild on every 10th), L2 flushed "
+                  "before each",
         "gpu_launches": int(launches),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(system.n * 12 + 4),
                 "d2h_bytes_per_step": CTL_BYTES,
@@ -288,9 +312,10 @@ def run_native(args) -> dict:
             "peak": pk["hbm_gbs"],
             "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"],
-            "traffic": STEP_KERNEL_TRAFFIC_BYTES,
-            "traffic_src": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
-                           "profiles/k_step_uniform_lj_100k.md",
+            "traffic": STEP_KERNEL_TRAFFIC["bytes"],
+            "traffic_src": f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch after an L2 flush, "
+                           f"captured {STEP_KERNEL_TRAFFIC['captured']}",
+            "traffic_stale": STEP_KERNEL_TRAFFIC["sources_sha"] != step_sources_sha(),
             "peak_src": pk["src"],
             "algorithmic_bytes_per_launch": alg["step_kernel_bytes"],
             "kernel_ms": kernel_s * 1e3,
@@ -514,9 +539,8 @@ def run_adjoint(reps: int = 5) -> dict:
 
 
 def run_case(name: str) -> dict:
-    """Small fixed drivers for profiling one kernel family (used by the ncu commands recorded
-    under profiles/): each sets up one workload, runs a few warm-up steps and then the launches
-    to capture."""
+    """Small fixed drivers for profiling one kernel family under ncu: each sets up one workload,
+    runs a few warm-up steps and then the launches to capture."""
     import torch
     from biospring_gb300 import SpringNetwork, workloads as W
 
@@ -568,47 +592,70 @@ def run_case(name: str) -> dict:
     raise SystemExit(f"unknown case {name}")
 
 
+def _oracle_steps_per_s(system, steps: int, warmup: int) -> tuple[float, float]:
+    """(particle-steps/s, seconds) of the CPU restatement on all host cores: `warmup` untimed
+    steps, then `steps` timed ones."""
+    from oracle import pyoracle
+    orc = pyoracle.Oracle(system)
+    for _ in range(warmup):
+        orc.time_steps(1)
+    t = orc.time_steps(steps)
+    orc.close()
+    return system.n * steps / t, t
+
+
 def cpu_baseline(system, seconds: float = 15.0) -> dict:
-    """The CPU restatement of the reference step on all host cores (OpenMP), bounded sample."""
+    """The CPU restatement of the reference step on all host cores (OpenMP), bounded sample of
+    the same workload; beside it the same sample with the constant dielectric (eps = 4), the
+    reference's own Coulomb form."""
     from oracle import pyoracle
     pyoracle.build_oracle()
     cores = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(cores)
-    orc = pyoracle.Oracle(system)
-    orc.time_steps(1)
-    t = orc.time_steps(1)
-    nsteps = max(1, min(30, int(seconds / max(t, 1e-3))))
-    t = orc.time_steps(nsteps)
-    orc.close()
-    return {"value": system.n * nsteps / t, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{nsteps} full steps of the 100k workload after 2 untimed ones"}
+    probe, t1 = _oracle_steps_per_s(system, 1, 1)
+    nsteps = max(1, min(30, int(seconds / max(t1, 1e-3))))
+    value, _ = _oracle_steps_per_s(system, nsteps, 2)
+    const = dict(system.config)
+    const["dielectric_mode"] = 0
+    cs = dataclasses.replace(system, config=const)
+    cvalue, _ = _oracle_steps_per_s(cs, max(1, nsteps // 3), 1)
+    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{nsteps} full steps of the 100k workload after 2 untimed ones",
+            "dielectric": "eps = 4r, as the native arm",
+            "constant_dielectric_value": cvalue}
+
+
+REFERENCE_MAX_STEPS = 300  # about a minute of the 100k step on 16 host cores
 
 
 def run_reference(args) -> dict | None:
+    """The reference arm: the CPU restatement (bit-exact with the reference's own step in constant
+    dielectric mode, and its eps = 4r extension here) on all host cores, on the native arm's
+    workload, config, metric and warm-up. Neither the system nor the configuration comes from a
+    product library: the oracle's library holds its own copy of the generators and its own
+    restatement of the reference's default parameters."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return None
     from oracle import pyoracle
     pyoracle.build_oracle()
+    pyoracle.use_oracle_generator()
     cores = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(cores)
     system = make_workload(seed=42)
-    orc = pyoracle.Oracle(system)
-    # a bounded sample: a 100k step takes about 0.2 s on 16 cores, so at most 200 timed steps
-    steps = min(args.steps, 200)
-    for _ in range(min(args.warmup, 5)):
-        orc.time_steps(1)
-    t = orc.time_steps(steps)
-    orc.close()
-    value = system.n * steps / t
+    steps = max(1, min(args.steps, REFERENCE_MAX_STEPS))
+    value, t = _oracle_steps_per_s(system, steps, args.warmup)
+    sample = (f"{steps} full steps after {args.warmup} untimed ones, OpenMP on all {cores} host cores"
+              + ("" if steps == args.steps else f" (bounded sample of the {args.steps} requested)"))
     return {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": steps, "warmup": args.warmup, "ms_per_step": t * 1e3 / steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": "uniform_lj_100k (same system as the native arm)", "global_batch": system.n},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform fill, springs, charges)",
+        "config": workload_config(system, world),
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{steps} full steps after {min(args.warmup, 5)} warm-up steps, OpenMP on all cores"},
+        "timing": "wall clock around the oracle's step loop (host code, no GPU)",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -631,13 +678,10 @@ def main():
             build.build_all()
         print(json.dumps(run_case(args.case)))
         return
+    args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
-        if args.steps > 20:
-            args.steps = 10  # a bounded CPU sample (each step is ~1 s of CPU work)
-        args.warmup = max(1, min(args.warmup, 3))
         out = run_reference(args)
     else:
-        args.warmup = max(args.warmup, 3)
         from biospring_gb300 import build
         if not os.path.exists(build.LIB):
             build.build_all()

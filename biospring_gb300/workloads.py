@@ -29,14 +29,23 @@ SYNTH_PATH = os.path.join(PKG, "libbs_synth.so")
 KCAL_TO_KJ = 4.1840  # src/forcefield/constants.hpp:46
 
 _synth = None
+_synth_path = SYNTH_PATH
+
+
+def set_generator_library(path: str) -> None:
+    """Takes the generators (the bs_synth_* functions of csrc/synth.cpp) from another shared
+    library built from the same source; the same seed gives the same system."""
+    global _synth, _synth_path
+    if path != _synth_path:
+        _synth, _synth_path = None, path
 
 
 def _lib():
     global _synth
     if _synth is None:
-        if not os.path.exists(SYNTH_PATH):
-            raise RuntimeError(f"{SYNTH_PATH} is missing: run the package build first")
-        lib = C.CDLL(SYNTH_PATH)
+        if not os.path.exists(_synth_path):
+            raise RuntimeError(f"{_synth_path} is missing: run the package build first")
+        lib = C.CDLL(_synth_path)
         lib.bs_synth_ca_chain.restype = C.c_double
         lib.bs_synth_ca_chain.argtypes = [C.c_int64, C.c_uint64, C.c_double, C.c_double, C.c_double,
                                           C.POINTER(C.c_float)]

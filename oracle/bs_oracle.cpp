@@ -1008,6 +1008,51 @@ struct Sim
 
 extern "C" {
 
+// The reference's default parameters (configuration::defaultConfiguration,
+// src/configuration/Configuration.hpp:153-234) in the bs_config layout, restated here so that
+// the oracle builds its configuration without the product library. Fields the reference does
+// not have take the values that make the step the reference's: constant dielectric, the
+// hard-coded membrane (src/forcefield/energy/imp.hpp:13-15), list rebuilt every 10 steps.
+void bso_default_config(bs_config * c)
+{
+    std::memset(c, 0, sizeof(*c));
+    c->nbsteps = -1;
+    c->timestep = 0.01;
+    c->neighborskin = 0.0;
+    c->spring_enable = 0;
+    c->spring_scale = 1.0;
+    c->steric_enable = 0;
+    c->steric_gridscale = 1.0;
+    c->steric_cutoff = 1.0;
+    c->steric_mode = BS_STERIC_LINEAR;
+    c->coulomb_enable = 0;
+    c->coulomb_scale = 1.0;
+    c->coulomb_cutoff = 16.0;
+    c->coulomb_dielectric = 1.0;
+    c->hydrophobicity_enable = 0;
+    c->hydrophobicity_scale = 1.0;
+    c->hydrophobicity_cutoff = 15.0;
+    c->impala_enable = 0;
+    c->impala_scale = 1.0;
+    c->viscosity_enable = 0;
+    c->viscosity_value = 1.0;
+    c->rigidbody_enable = 0;
+    c->dielectric_mode = BS_DIELECTRIC_CONSTANT;
+    c->impala_z0 = 15.75;
+    c->impala_alpha = 1.99;
+    c->rebuild_every = 10;
+    c->list_skin = 1.0;
+    c->probe_x = 1.0;
+    c->probe_y = 1.0;
+    c->probe_z = 1.0;
+    c->probe_mass = 1.0;
+    c->probe_epsilon = 1.0;
+    c->probe_radius = 1.0;
+    c->probe_charge = 0.0;
+    c->potentialgrid_scale = 1.0;
+    c->densitygrid_scale = 1.0;
+}
+
 void * bso_create(const bs_config * cfg, int64_t n, const float * xyz, const float * vel, const float * mass,
                   const float * charge, const float * radius, const float * eps, const float * hydro,
                   const float * sasa, const float * transfer, const uint8_t * is_static, int64_t ns,

@@ -22,8 +22,14 @@ ORACLE_SO = os.path.join(HERE, "libbs_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libbsref.so")
 
 
+# The seeded generators of the synthetic systems (host C++, no CUDA) are compiled into the
+# oracle's library as well, so that a CPU run builds its system without mapping any product
+# library; the same source and seed give the same coordinates.
+SYNTH_SRC = os.path.join(os.path.dirname(HERE), "biospring_gb300", "csrc", "synth.cpp")
+
+
 def build_oracle() -> str:
-    srcs = [os.path.join(HERE, "bs_oracle.cpp"), os.path.join(HERE, "adjoint_fp64.cpp")]
+    srcs = [os.path.join(HERE, "bs_oracle.cpp"), os.path.join(HERE, "adjoint_fp64.cpp"), SYNTH_SRC]
     hdr = os.path.join(os.path.dirname(HERE), "include", "biospring_gb300.h")
     if (not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < max([os.path.getmtime(f) for f in srcs] +
                                                                            [os.path.getmtime(hdr)])):
@@ -54,6 +60,27 @@ def reference_dir() -> str:
 
 def have_reference() -> bool:
     return os.path.exists(REF_SO)
+
+
+def use_oracle_generator() -> None:
+    """Makes biospring_gb300.workloads generate systems with the oracle library's copy of the
+    generators (no product library is loaded)."""
+    from biospring_gb300 import workloads
+    workloads.set_generator_library(build_oracle())
+
+
+def oracle_config(system):
+    """The system's run parameters over the reference's defaults as the oracle restates them
+    (bso_default_config), without the product library."""
+    from biospring_gb300.capi import BsConfig
+    lib = C.CDLL(build_oracle())
+    lib.bso_default_config.restype = None
+    lib.bso_default_config.argtypes = [C.POINTER(BsConfig)]
+    cfg = BsConfig()
+    lib.bso_default_config(C.byref(cfg))
+    for key, v in system.config.items():
+        setattr(cfg, key, v)
+    return cfg
 
 
 _f32p = C.POINTER(C.c_float)
@@ -120,7 +147,7 @@ class _CpuSim:
 
     def __init__(self, system, cfg=None):
         f = self._load()
-        cfg = system.bs_config() if cfg is None else cfg
+        cfg = oracle_config(system) if cfg is None else cfg
         self.cfg = cfg
         a = {k: (None if v is None else np.ascontiguousarray(v)) for k, v in system.arrays().items()}
         self._keep = a
@@ -285,7 +312,7 @@ def _adj_lib():
 
 
 def _adj_args(system, nsteps, target):
-    cfg = system.bs_config()
+    cfg = oracle_config(system)
     a = system.arrays()
     f32 = lambda v: None if v is None else np.ascontiguousarray(v, np.float32)  # noqa: E731
     keep = dict(xyz=f32(a["xyz"]).reshape(-1), vel=f32(a["vel"]), mass=f32(a["mass"]), radius=f32(a["radius"]),

@@ -38,9 +38,18 @@ def build_oracle() -> str:
     return ORACLE_SO
 
 
+# Where this container mounts the reference's sources; $REF overrides it. The GPU machines have
+# no copy, and there nothing is built from it.
+DEFAULT_REF = "/root/reference"
+
+
 def build_reference() -> str | None:
     """Builds oracle/_ref/libbsref.so when the reference sources are present (make -f oracle/ref.mk)."""
-    proc = subprocess.run(["make", "-s", "-f", os.path.join(HERE, "ref.mk"), f"-j{os.cpu_count() or 4}"],
+    ref = reference_dir()
+    if not ref:
+        return REF_SO if os.path.exists(REF_SO) else None
+    proc = subprocess.run(["make", "-s", "-f", os.path.join(HERE, "ref.mk"), f"REF={ref}",
+                           f"-j{os.cpu_count() or 4}"],
                           cwd=os.path.dirname(HERE), stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if proc.returncode != 0:
         raise RuntimeError("reference build failed:\n" + proc.stdout[-4000:])
@@ -48,14 +57,10 @@ def build_reference() -> str | None:
 
 
 def reference_dir() -> str:
-    """The reference source tree the recipe oracle/ref.mk builds from (its REF, or $REF)."""
-    if os.environ.get("REF"):
-        return os.environ["REF"]
-    with open(os.path.join(HERE, "ref.mk")) as f:
-        for line in f:
-            if line.startswith("REF ?="):
-                return line.split("=", 1)[1].strip()
-    return ""
+    """The reference source tree: $REF, else the default mount when it holds the sources; empty
+    where there is none."""
+    ref = os.environ.get("REF") or DEFAULT_REF
+    return ref if os.path.exists(os.path.join(ref, "src", "spn", "SpringNetwork.cpp")) else ""
 
 
 def have_reference() -> bool:

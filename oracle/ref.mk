@@ -2,7 +2,10 @@
 # lie, into oracle/_ref/ (git-ignored). Test infrastructure only: it pins the CPU
 # restatement and generates golden fixtures; the product never links it.
 #
-#   make -f oracle/ref.mk REF=/root/reference -j8
+#   make -f oracle/ref.mk REF=<reference source tree> -j8
+#
+# REF is required (command line or environment): without it, or where it holds no sources,
+# nothing is built.
 #
 # The list is the reference's BIOSPRING_CORE_SOURCES (CMakeLists.txt:131-175) minus
 # src/IO/io.cpp and src/IO/NetCDF*.cpp, which need the absent NetCDF library and are
@@ -12,7 +15,7 @@
 # build (-O2 -fopenmp -DOPENMP_SUPPORT, C++20). -ffp-contract=off keeps float
 # arithmetic identical on x86-64 and aarch64.
 
-REF ?= /root/reference
+REF ?=
 HERE := $(dir $(lastword $(MAKEFILE_LIST)))
 OUT := $(HERE)_ref
 OBJ := $(OUT)/obj
@@ -71,7 +74,7 @@ CORE_OBJS := $(foreach s,$(CORE),$(call objname,$(s)))
 XDR_OBJS := $(foreach s,$(XDR),$(call objname,$(s)))
 DRIVER_OBJ := $(OBJ)/ref_driver.o
 
-ifeq ($(wildcard $(REF)/src/spn/SpringNetwork.cpp),)
+ifeq ($(and $(REF),$(wildcard $(REF)/src/spn/SpringNetwork.cpp)),)
 all:
 	@echo "reference sources not present: oracle/_ref is not built"
 else

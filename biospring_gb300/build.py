@@ -25,7 +25,7 @@ SYNTH = os.path.join(PKG, "libbs_synth.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["bs_kernels.cu", "bs_batch.cu", "bs_adjoint.cu", "bs_rigid.cu", "bs_capi.cu", "bs_noalloc.cu"]
-HOST_SOURCES = ["bs_msp.cpp", "bs_field.cpp", "bs_nc.cpp"]
+HOST_SOURCES = ["bs_msp.cpp", "bs_field.cpp", "bs_nc.cpp", "bs_xtc.cpp"]
 
 
 def _nvcc() -> str:

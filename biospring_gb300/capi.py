@@ -154,6 +154,12 @@ SIGNATURES = {
     "bs_set_batch_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "bs_get_batch_shape": (C.c_int, [C.c_void_p, _i32p]),
     "bs_batch_autotune": (C.c_int, [C.c_void_p, _i32p]),
+    "bs_xtc_frame_bound": (C.c_int, [C.c_int64, C.POINTER(C.c_size_t)]),
+    "bs_xtc_encode_frame": (C.c_int, [C.c_int64, C.c_int32, C.c_float, _f32p, _f32p, C.c_float,
+                                      C.POINTER(C.c_uint8), C.c_size_t, C.POINTER(C.c_size_t)]),
+    "bs_xtc_decode_frame": (C.c_int, [C.POINTER(C.c_uint8), C.c_size_t, C.c_int64, C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_float), _f32p, _f32p, C.POINTER(C.c_float),
+                                      C.POINTER(C.c_size_t)]),
 }
 
 _lib = None
@@ -225,6 +231,39 @@ def read_nc(path: str) -> dict:
         if not flag:
             out[key] = None
     return out
+
+
+def xtc_encode(xyz_nm, step: int, time: float, box=None, precision: float = 1000.0) -> bytes:
+    """One XTC frame (bs_xtc_encode_frame) of float (n, 3) coordinates in nm."""
+    lib = load()
+    x = np.ascontiguousarray(xyz_nm, np.float32).reshape(-1, 3)
+    n = x.shape[0]
+    cap = C.c_size_t()
+    lib.bs_xtc_frame_bound(n, C.byref(cap))
+    out = np.zeros(cap.value, np.uint8)
+    size = C.c_size_t()
+    b = None if box is None else np.ascontiguousarray(box, np.float32).reshape(9)
+    rc = lib.bs_xtc_encode_frame(n, int(step), float(time), ptr(b, C.c_float), ptr(x, C.c_float), float(precision),
+                                 out.ctypes.data_as(C.POINTER(C.c_uint8)), cap.value, C.byref(size))
+    if rc != BS_OK:
+        raise BsError(rc, "bs_xtc_encode_frame failed (coordinates too large for the precision?)")
+    return out[:size.value].tobytes()
+
+
+def xtc_decode(data: bytes, natoms: int, offset: int = 0) -> dict:
+    """One XTC frame of natoms atoms read from data[offset:] (bs_xtc_decode_frame)."""
+    lib = load()
+    buf = np.frombuffer(data, np.uint8)[offset:]
+    buf = np.ascontiguousarray(buf)
+    xyz = np.zeros((natoms, 3), np.float32)
+    box = np.zeros(9, np.float32)
+    step, t, prec, used = C.c_int32(), C.c_float(), C.c_float(), C.c_size_t()
+    rc = lib.bs_xtc_decode_frame(buf.ctypes.data_as(C.POINTER(C.c_uint8)), buf.shape[0], natoms, C.byref(step),
+                                 C.byref(t), ptr(box, C.c_float), ptr(xyz, C.c_float), C.byref(prec), C.byref(used))
+    if rc != BS_OK:
+        raise BsError(rc, "bs_xtc_decode_frame: not a valid XTC frame of that many atoms")
+    return dict(step=step.value, time=t.value, box=box.reshape(3, 3), xyz=xyz, precision=prec.value,
+                consumed=used.value)
 
 
 def parse_msp(text: str, base: BsConfig | None = None) -> BsConfig:

@@ -1,10 +1,11 @@
 """Trajectory and energy output from the frame recorder (bs_set_frames / bs_read_frames).
 
 The device writes frames into a host ring while it steps; :class:`FrameWriter` drains the ring on a
-background thread and appends each frame to a PDB trajectory (one MODEL per frame) and its
-energies to a tab-separated table laid out like the reference's CSV sampling (step, frame rate,
-then one column per enabled energy term; src/IO/CSVSampleWriter.cpp), so the stepping loop never
-waits for file output.
+background thread and appends each frame to a PDB trajectory (one MODEL per frame), to an XTC
+trajectory (bs_xtc_encode_frame, with the reference's conventions: src/IO/modern/
+XTCTrajectoryWriter.cpp:15-32) and its energies to a tab-separated table laid out like the
+reference's CSV sampling (step, frame rate, then one column per enabled energy term;
+src/IO/CSVSampleWriter.cpp), so the stepping loop never waits for file output.
 """
 
 from __future__ import annotations
@@ -45,6 +46,14 @@ def pdb_model(model: int, xyz: np.ndarray, names=None, resnames=None, resids=Non
     return "\n".join(lines) + "\n"
 
 
+def xtc_frame(frame: int, xyz_angstrom: np.ndarray) -> bytes:
+    """One XTC frame as the reference's XTC writer makes it: coordinates divided by 10 in double
+    and stored as float (nm), an identity box, the writer's frame counter (from 0) as step and
+    time, precision 1000."""
+    nm = (np.asarray(xyz_angstrom, np.float32).astype(np.float64) / 10.0).astype(np.float32)
+    return capi.xtc_encode(nm, int(frame), float(frame), np.eye(3, dtype=np.float32), 1000.0)
+
+
 def energy_header(terms) -> str:
     return "\t".join(["# Step", "FrameRate(Hz)"] + [ENERGY_LABELS[t] for t in terms]) + "\n"
 
@@ -69,10 +78,11 @@ class FrameWriter:
     energy table. Call :meth:`close` after the last step (it takes the frames still in the ring)."""
 
     def __init__(self, net, pdb_path=None, energy_path=None, terms=None, poll: float = 0.002, names=None,
-                 resnames=None, resids=None, chains=None):
+                 resnames=None, resids=None, chains=None, xtc_path=None):
         self.net = net
         self.terms = terms or ["kinetic", "spring", "steric", "electrostatic", "imp", "hydrophobic"]
         self.pdb = open(pdb_path, "w") if pdb_path else None
+        self.xtc = open(xtc_path, "wb") if xtc_path else None
         self.csv = open(energy_path, "w") if energy_path else None
         if self.csv:
             self.csv.write(energy_header(self.terms))
@@ -96,6 +106,8 @@ class FrameWriter:
             self.frames += 1
             if self.pdb:
                 self.pdb.write(pdb_model(self.frames, xyz[k], **self.meta))
+            if self.xtc:
+                self.xtc.write(xtc_frame(self.frames - 1, xyz[k]))
             if self.csv:
                 self.csv.write(energy_row(steps[k], rate, en[k], self.terms))
         return len(steps)
@@ -111,7 +123,7 @@ class FrameWriter:
         self.net.synchronize()
         while self._drain():
             pass
-        for f in (self.pdb, self.csv):
+        for f in (self.pdb, self.csv, self.xtc):
             if f:
                 f.close()
         return self.frames, self.dropped

@@ -295,6 +295,21 @@ int bs_set_external_forces(bs_sim *sim, const float *f);
  * particles but does not move it. */
 int bs_get_probe(bs_sim *sim, float state[6]);
 
+/* XTC trajectory frames, host code (no device involved). The reference writes XTC through its
+ * vendored xdrfile library: src/IO/modern/XTCTrajectoryWriter.cpp:15-32 (write_xtc with the
+ * coordinates in nm, an identity box, the frame counter as step and time, precision 1000;
+ * selected at src/spn/SpringNetwork.cpp:768-779). bs_xtc_encode_frame writes one frame of
+ * natoms coordinates (float[3 natoms], nm) into out (cap bytes) and its size into *len
+ * (BS_E_CAPACITY, with *len set, when it does not fit); box is float[9] (NULL: identity).
+ * bs_xtc_frame_bound gives a capacity that always fits. bs_xtc_decode_frame reads one frame of
+ * natoms atoms from in, returning its step, time, box, coordinates, precision (0 for frames of at
+ * most 9 atoms, stored uncompressed) and the bytes it used (each output nullable except xyz). */
+int bs_xtc_frame_bound(int64_t natoms, size_t *bytes);
+int bs_xtc_encode_frame(int64_t natoms, int32_t step, float time, const float box[9], const float *xyz,
+                        float precision, uint8_t *out, size_t cap, size_t *len);
+int bs_xtc_decode_frame(const uint8_t *in, size_t len, int64_t natoms, int32_t *step, float *time, float box[9],
+                        float *xyz, float *precision, size_t *consumed);
+
 /* Energies of the last step or force evaluation, BS_ENERGY_* order, in kJ/mol
  * (SpringNetwork::getKineticEnergy ... getHydrophobicEnergy, SpringNetwork.h:157-162).
  * They are reduced in FP64 on the device. */
@@ -385,9 +400,11 @@ int bs_batch_autotune(bs_sim *sim, int32_t shape[3]);
  *
  * n outside [1, BS_NOALLOC_MAX_PARTICLES] returns BS_E_ARG. The first call on a device
  * sets up the scratch (it loads the kernels onto that device) and should come before
- * any stream capture. All calls on one device share the scratch: two calls in flight
- * at once (other streams, other threads) race; order them on one stream. err
- * (nullable) receives a one-line message on failure. */
+ * any stream capture. The scratch address found then is kept for the life of the
+ * process, so calls after a cudaDeviceReset of that device are not supported. All
+ * calls on one device share the scratch: two calls in flight at once (other streams,
+ * other threads) race; order them on one stream. err (nullable) receives a one-line
+ * message on failure. */
 #define BS_NOALLOC_MAX_PARTICLES 16384
 int bs_nonbonded_forces_noalloc(const bs_config *cfg, int64_t n, const float *d_xyz,
                                 const float *d_radius, const float *d_epsilon,

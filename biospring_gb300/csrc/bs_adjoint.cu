@@ -383,10 +383,15 @@ __global__ void k_adj_combine(int nsp, const float *gk, const float *gr0, float 
 
 int launch_adj_step(const Params &p, const AdjState &a, cudaStream_t st)
 {
-    // the forward step's lanes per particle (more lanes for small systems: more warps in flight)
-    const int T = p.step_lanes >= 8 ? 8 : (p.step_lanes == 2 ? 2 : 4);
+    // Lanes per particle: a backward step does about twice the forward's work per spring and
+    // pair (Hessian-vector products, gradient sums) on a grid of the same size, so small systems
+    // take 16 lanes (10,000 particles: 160,000 threads, 8 blocks of 128 per SM) to keep enough
+    // loads in flight; larger ones follow the forward step.
+    const int T = p.n < 20000 ? 16 : (p.step_lanes >= 8 ? 8 : (p.step_lanes == 2 ? 2 : 4));
     const int nb = static_cast<int>((static_cast<long long>(p.npad) * T + kStepBlock - 1) / kStepBlock);
-    if (T == 8)
+    if (T == 16)
+        k_adj_step<16><<<nb, kStepBlock, 0, st>>>(p, a);
+    else if (T == 8)
         k_adj_step<8><<<nb, kStepBlock, 0, st>>>(p, a);
     else if (T == 2)
         k_adj_step<2><<<nb, kStepBlock, 0, st>>>(p, a);

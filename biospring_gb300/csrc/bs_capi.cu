@@ -114,7 +114,9 @@ struct bs_sim
     double *adj_blk = nullptr, *adj_loss = nullptr;
     unsigned int *adj_done = nullptr;
     cudaGraphExec_t adj_graph = nullptr;
-    int adj_key[3] = {0, 0, 0};
+    int adj_key[4] = {0, 0, 0, 0};
+    // double membrane: upper offset, lower offset, upper and lower tube curvatures (bs_set_membrane)
+    float memb[4] = {0.f, 0.f, 0.f, 0.f};
     float *adj_gq = nullptr; // dL/dq per caller id
     long long adj_kernels = 0;
     // diagnostics scratch
@@ -264,7 +266,9 @@ int alloc_lists(bs_sim *s, const int caps[kLists], int cell_cap)
     free_growable(s);
     for (int t = 0; t < kLists; ++t)
     {
-        const int cap = p.pl[t].on ? std::max(caps[t], 1) : 1;
+        // a multiple of 8 entries, so every row starts on a 16-byte boundary (vector loads of the
+        // step kernel read 4 entries at a time)
+        const int cap = p.pl[t].on ? (std::max(caps[t], 1) + 7) / 8 * 8 : 8;
         BS_CUDA(cudaMalloc(reinterpret_cast<void **>(&s->pl_idx[t]),
                            static_cast<size_t>(p.npad) * cap * sizeof(unsigned int)));
         p.pl[t].idx = s->pl_idx[t];
@@ -498,6 +502,17 @@ int enqueue_batch(bs_sim *s, long long count, bool catchup)
     }
     BS_CUDA(cudaGetLastError());
     return BS_OK;
+}
+
+// The double membrane into the step parameters (flat when every value is zero).
+void apply_membrane(bs_sim *s)
+{
+    Params &p = s->p;
+    p.imp_off[0] = s->memb[0];
+    p.imp_off[1] = -s->memb[1];
+    p.imp_curv[0] = s->memb[2];
+    p.imp_curv[1] = s->memb[3];
+    p.imp_double = (s->memb[0] != 0.f || s->memb[1] != 0.f || s->memb[2] != 0.f || s->memb[3] != 0.f) ? 1 : 0;
 }
 
 } // namespace
@@ -844,6 +859,24 @@ int bs_get_field_grid(bs_sim *s, int32_t which, int32_t shape[3], float *out)
     return BS_OK;
 }
 
+int bs_set_membrane(bs_sim *s, float upper_offset, float lower_offset, float upper_curvature,
+                    float lower_curvature)
+{
+    if (!s)
+        return fail(nullptr, BS_E_ARG, "null handle");
+    if (!std::isfinite(upper_offset) || !std::isfinite(lower_offset) || !std::isfinite(upper_curvature) ||
+        !std::isfinite(lower_curvature))
+        return fail(s, BS_E_ARG, "bs_set_membrane: offsets and curvatures must be finite");
+    BS_CUDA(cudaStreamSynchronize(s->stream)); // no step in flight uses the old parameters
+    s->memb[0] = upper_offset;
+    s->memb[1] = lower_offset;
+    s->memb[2] = upper_curvature;
+    s->memb[3] = lower_curvature;
+    apply_membrane(s);
+    destroy_graph(s); // the captured periods hold the old parameters
+    return BS_OK;
+}
+
 int bs_set_burying(bs_sim *s, const float *burying)
 {
     if (!s)
@@ -1042,6 +1075,11 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
         flags0[i] = flags;
         iprm0[i] = make_float4(s->mass[i], s->sasa[i], s->transfer[i], 0.f);
     }
+    p.lj_uniform = n > 0 ? 1 : 0;
+    for (int64_t i = 1; i < n && p.lj_uniform; ++i)
+        if (fhi0[i] != fhi0[0])
+            p.lj_uniform = 0;
+    p.lj_F = n > 0 ? fhi0[0] : 0.0f;
     std::vector<int> perm0(npad, 0), inv0(n);
     for (int64_t i = 0; i < n; ++i)
     {
@@ -1413,6 +1451,7 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     p.visc = static_cast<float>(c.viscosity_value);
     p.imp_z0 = static_cast<float>(c.impala_z0);
     p.imp_alpha = static_cast<float>(c.impala_alpha);
+    apply_membrane(s);
     const double D = static_cast<float>(c.coulomb_dielectric);
     const double cs = static_cast<float>(c.coulomb_scale);
     p.k_spring_f = static_cast<float>(kSpringForceConvert);
@@ -2136,7 +2175,11 @@ int bs_set_spring_parameters(bs_sim *s, const float *stiffness, const float *equ
 
 // Records the whole adjoint run (forward with checkpoints, then the backward sweep with
 // recomputation from each checkpoint) on the handle's stream.
-static int record_adjoint(bs_sim *s, int nsteps, int K, bool charges)
+// keep_all: the positions of every step of every interval are kept from the first forward pass
+// (they fit the memory budget), so the backward pass restores each interval's layout with one
+// rebuild from its checkpoint and recomputes no step; otherwise only the last interval's are kept
+// and each earlier interval is recomputed from its checkpoint.
+static int record_adjoint(bs_sim *s, int nsteps, int K, bool charges, bool keep_all)
 {
     Params &p = s->p;
     const int S = (nsteps + K - 1) / K;
@@ -2158,8 +2201,11 @@ static int record_adjoint(bs_sim *s, int nsteps, int K, bool charges)
         s->launches += launch_rebuild(p, s->stream);
         for (int k = 0; k < seg_len(seg); ++k)
         {
-            if (seg == S - 1)
-                s->launches += launch_adj_save(p, s->adj_seg + k * np, lo_seg ? lo_seg + k * np : nullptr, s->stream);
+            if (keep_all || seg == S - 1)
+            {
+                const size_t at = (keep_all ? static_cast<size_t>(seg) * K + k : static_cast<size_t>(k)) * np;
+                s->launches += launch_adj_save(p, s->adj_seg + at, lo_seg ? lo_seg + at : nullptr, s->stream);
+            }
             s->launches += launch_step(p, MODE_STEP, s->stream);
         }
     }
@@ -2177,7 +2223,7 @@ static int record_adjoint(bs_sim *s, int nsteps, int K, bool charges)
             s->launches += launch_set_positions(p, s->adj_ck_xyz + seg * n3, s->adj_ck_vel + seg * n3, s->stream,
                                                 p.pos_lo[0] ? s->adj_ck_lo + seg * n3 : nullptr);
             s->launches += launch_rebuild(p, s->stream);
-            for (int k = 0; k < len; ++k)
+            for (int k = 0; !keep_all && k < len; ++k)
             {
                 s->launches += launch_adj_save(p, s->adj_seg + k * np, lo_seg ? lo_seg + k * np : nullptr,
                                                s->stream);
@@ -2188,8 +2234,9 @@ static int record_adjoint(bs_sim *s, int nsteps, int K, bool charges)
         }
         for (int k = len - 1; k >= 0; --k)
         {
-            a.x = s->adj_seg + k * np;
-            a.xlo = lo_seg ? lo_seg + k * np : nullptr;
+            const size_t at = (keep_all ? static_cast<size_t>(seg) * K + k : static_cast<size_t>(k)) * np;
+            a.x = s->adj_seg + at;
+            a.xlo = lo_seg ? lo_seg + at : nullptr;
             a.nu_in = s->adj_nu[cur];
             a.nu_out = s->adj_nu[cur ^ 1];
             s->launches += launch_adj_step(p, a, s->stream);
@@ -2250,6 +2297,17 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
     const int S = (nsteps + K - 1) / K;
     const size_t n3 = 3 * static_cast<size_t>(s->n), np = static_cast<size_t>(p.npad);
     const size_t ns = s->sp_i.size();
+    // Positions of every step kept when they take at most a quarter of the free device memory
+    // (10,000 particles x 200 steps: 32 MB, twice that with precise positions).
+    bool keep_all = false;
+    {
+        size_t free_b = 0, total_b = 0;
+        BS_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        const double per_step = static_cast<double>(np) * sizeof(float4) * (p.pos_lo[0] ? 2.0 : 1.0);
+        const double held = static_cast<double>(s->adj_seg_cap) * per_step;
+        keep_all = static_cast<double>(nsteps) * per_step <= 0.25 * (static_cast<double>(free_b) + held);
+    }
+    const int seg_cap = keep_all ? nsteps : K;
     // directed spring ids in the sorted spring table (filled by every rebuild from now on)
     if (!p.se_sid)
     {
@@ -2263,12 +2321,12 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
         s->sp_sid_d = d_sid;
         destroy_graph(s);
     }
-    if (S > s->adj_ck_cap || K > s->adj_seg_cap || !s->adj_lx)
+    if (S > s->adj_ck_cap || seg_cap > s->adj_seg_cap || !s->adj_lx)
     {
         destroy_graph(s);
         // (buffers of a smaller earlier run stay allocated until the handle is set up again)
         s->adj_ck_cap = std::max(S, s->adj_ck_cap);
-        s->adj_seg_cap = std::max(K, s->adj_seg_cap);
+        s->adj_seg_cap = std::max(seg_cap, s->adj_seg_cap);
         BS_CUDA(s->dev.alloc(&s->adj_ck_xyz, s->adj_ck_cap * n3));
         BS_CUDA(s->dev.alloc(&s->adj_ck_vel, s->adj_ck_cap * n3));
         BS_CUDA(s->dev.alloc(&s->adj_ck_lo, s->adj_ck_cap * n3));
@@ -2305,7 +2363,8 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
     const Ctl saved = *s->ctl_host;
     for (int attempt = 0; attempt < 4; ++attempt)
     {
-        if (!s->adj_graph || s->adj_key[0] != nsteps || s->adj_key[1] != K || s->adj_key[2] != (charges ? 1 : 0))
+        if (!s->adj_graph || s->adj_key[0] != nsteps || s->adj_key[1] != K || s->adj_key[2] != (charges ? 1 : 0) ||
+            s->adj_key[3] != (keep_all ? 1 : 0))
         {
             if (s->adj_graph)
             {
@@ -2318,7 +2377,7 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
             // the adjoint's forward runs record no frames
             const int frame_every = s->p.frame_every;
             s->p.frame_every = 0;
-            rc = record_adjoint(s, nsteps, K, charges);
+            rc = record_adjoint(s, nsteps, K, charges, keep_all);
             s->p.frame_every = frame_every;
             const cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
             if (rc)
@@ -2336,6 +2395,7 @@ int bs_adjoint(bs_sim *s, int32_t nsteps, int32_t checkpoint, const float *targe
             s->adj_key[0] = nsteps;
             s->adj_key[1] = K;
             s->adj_key[2] = charges ? 1 : 0;
+            s->adj_key[3] = keep_all ? 1 : 0;
             s->adj_kernels = s->launches - before;
             s->launches = before;
         }

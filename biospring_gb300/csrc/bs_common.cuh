@@ -185,6 +185,8 @@ struct Params
     // nonbonded pair lists
     PairList pl[kLists];
     int pl16;                 // list 0 holds 16-bit offsets
+    int lj_uniform;           // every particle has the same second steric factor, lj_F (one LJ type):
+    float lj_F;               // the step kernel then reads no per-partner factor
     // search grid
     int *cell_of;             // [npad] cell of each sorted slot (new layout)
     int *cell_cnt;            // [cell_cap + 1]
@@ -211,6 +213,9 @@ struct Params
     float spring_scale, steric_scale, coulomb_scale, hydro_scale, imp_scale;
     float visc;
     float imp_z0, imp_alpha;
+    int imp_double;           // the double membrane (any offset or tube curvature set)
+    float imp_off[2];         // signed offsets of the upper (+) and lower (-) membranes
+    float imp_curv[2];        // their tube curvatures (1/A; 0 flat)
     float k_spring_f;         // (float) kSpringForceConvert
     float k_elec_e;           // kCoulombEnergyPerA / dielectric
     float k_elec_f;           // kElecForceConvert / (4 pi dielectric)

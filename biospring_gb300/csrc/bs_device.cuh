@@ -413,6 +413,229 @@ __device__ __forceinline__ void steric_forces(const Params &p, int s, int t, flo
     }
 }
 
+// The LJ pair body of steric_forces: adds the pair's weighted energy to e and returns the force
+// over distance (both zero for a rejected pair). ok says whether the pair is in the cutoff.
+template <int SM>
+__device__ __forceinline__ float lj_pair(float r2, bool ok, float pw, float fhi_i, float4 pj, float hj, float w,
+                                         float &e)
+{
+    const float inv2 = recip_nr(r2);
+    const float i6 = inv2 * inv2 * inv2;
+    const float t6 = pw * pj.w * i6;
+    float fod, de;
+    if (SM == BS_STERIC_LJ_12_6_AMBER)
+    {
+        const float t12 = fhi_i * hj * i6 * i6;
+        de = t12 - 2.0f * t6;
+        fod = 12.0f * (t6 - t12) * inv2;
+    }
+    else if (SM == BS_STERIC_LJ_8_6_LEWITT)
+    {
+        const float t8 = fhi_i * hj * i6 * inv2;
+        de = 3.0f * t8 - 4.0f * t6;
+        fod = 24.0f * (t6 - t8) * inv2;
+    }
+    else
+    {
+        const float t8 = fhi_i * hj * i6 * inv2;
+        de = t8 - t6;
+        fod = (6.0f * t6 - 8.0f * t8) * inv2;
+    }
+    e = fmaf(w, ok ? de : 0.0f, e);
+    return ok ? fod : 0.0f;
+}
+
+// Steric pairs of slot s with its dynamic partners (list 0), lane t of T, in passes of kGatherU
+// consecutive entries per lane: lane t takes entries [base + U t, base + U t + U) with one vector
+// load of the row (U offsets of 16 bits, or U slots), then issues the U partners' position and LJ
+// factor loads together before any of them is used, so U gathers are in flight per lane and a
+// warp waits for one round trip per U pairs instead of one per pair. Entries past the row's end
+// are replaced by the slot itself and rejected. Rows start on 16-byte boundaries (capacities are
+// multiples of 8 entries), so the vector loads are aligned and never leave the row's capacity.
+template <int SM, int T, bool PL16, bool UF = false>
+__device__ __forceinline__ void steric_forces_batched(const Params &p, int s, int t, float4 pi, float fhi_i,
+                                                      const float4 *__restrict__ pos, const float *__restrict__ fhi,
+                                                      float &fx, float &fy, float &fz, float &e)
+{
+    constexpr int U = kGatherU;
+    static_assert(U == 4, "one 8-byte (16-bit mode) or 16-byte (32-bit mode) load per pass");
+    const PairList &L = p.pl[0];
+    const int cnt = L.cnt[s];
+    const size_t row = static_cast<size_t>(s) * L.cap;
+    const float lo2 = p.lo2_s, hi2 = p.hi2_s;
+    constexpr bool LJ = SM != BS_STERIC_LINEAR;
+    // BS_GATHER 3: the next pass's entries are loaded before this pass's partners, so the entry
+    // load of a pass overlaps the previous pass instead of preceding its partner loads.
+    uint2 w16n = make_uint2(0u, 0u);
+    uint4 w32n = make_uint4(0u, 0u, 0u, 0u);
+    if (BS_GATHER == 3 && U * t < cnt)
+    {
+        if (PL16)
+            w16n = __ldg(reinterpret_cast<const uint2 *>(reinterpret_cast<const short *>(L.idx) + row + U * t));
+        else
+            w32n = __ldg(reinterpret_cast<const uint4 *>(L.idx + row + U * t));
+    }
+    for (int base = (BS_GATHER == 2 ? t : U * t); base < cnt; base += U * T)
+    {
+        int j[U];
+        if (BS_GATHER == 3)
+        {
+            const uint2 w16 = w16n;
+            const uint4 w32 = w32n;
+            if (base + U * T < cnt)
+            {
+                if (PL16)
+                    w16n = __ldg(reinterpret_cast<const uint2 *>(reinterpret_cast<const short *>(L.idx) + row + base + U * T));
+                else
+                    w32n = __ldg(reinterpret_cast<const uint4 *>(L.idx + row + base + U * T));
+            }
+            if (PL16)
+            {
+                j[0] = s + static_cast<int>(static_cast<short>(w16.x & 0xffffu));
+                j[1] = s + (static_cast<int>(w16.x) >> 16);
+                j[2] = s + static_cast<int>(static_cast<short>(w16.y & 0xffffu));
+                j[3] = s + (static_cast<int>(w16.y) >> 16);
+            }
+            else
+            {
+                j[0] = static_cast<int>(w32.x & kSlotMask);
+                j[1] = static_cast<int>(w32.y & kSlotMask);
+                j[2] = static_cast<int>(w32.z & kSlotMask);
+                j[3] = static_cast<int>(w32.w & kSlotMask);
+            }
+        }
+        else if (BS_GATHER == 2)
+        {
+            // interleaved: entries base + T u, so at each u the T lanes of the particle read
+            // consecutive entries (neighbouring partner slots, often one cache line)
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+            {
+                const int k = min(base + T * u, cnt - 1);
+                if (PL16)
+                    j[u] = s + static_cast<int>(__ldg(reinterpret_cast<const short *>(L.idx) + row + k));
+                else
+                    j[u] = static_cast<int>(__ldg(L.idx + row + k) & kSlotMask);
+            }
+        }
+        else if (PL16)
+        {
+            const uint2 w = __ldg(reinterpret_cast<const uint2 *>(reinterpret_cast<const short *>(L.idx) + row + base));
+            j[0] = s + static_cast<int>(static_cast<short>(w.x & 0xffffu));
+            j[1] = s + (static_cast<int>(w.x) >> 16);
+            j[2] = s + static_cast<int>(static_cast<short>(w.y & 0xffffu));
+            j[3] = s + (static_cast<int>(w.y) >> 16);
+        }
+        else
+        {
+            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(L.idx + row + base));
+            j[0] = static_cast<int>(w.x & kSlotMask);
+            j[1] = static_cast<int>(w.y & kSlotMask);
+            j[2] = static_cast<int>(w.z & kSlotMask);
+            j[3] = static_cast<int>(w.w & kSlotMask);
+        }
+        float4 pj[U];
+        float hj[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+        {
+            if ((BS_GATHER == 2 ? base + T * u : base + u) >= cnt)
+                j[u] = s; // past the row: a stale entry; the slot itself is read instead
+            pj[u] = __ldg(&pos[j[u]]);
+            hj[u] = LJ ? (UF ? p.lj_F : __ldg(&fhi[j[u]])) : 0.0f; // one LJ type: no factor to gather
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+        {
+            const bool inrow = (BS_GATHER == 2 ? base + T * u : base + u) < cnt;
+            const float dx = pj[u].x - pi.x, dy = pj[u].y - pi.y, dz = pj[u].z - pi.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (SM == BS_STERIC_LINEAR)
+            {
+                if (!inrow || r2 >= hi2)
+                    continue;
+                if (!(r2 < lo2 && r2 > 1e-20f) && !exact_pair_test(pi, pj[u], p.c_steric, false))
+                    continue;
+                const float d = sqrtf(r2);
+                const float inv = d > 0.0f ? 1.0f / d : 0.0f;
+                const float dv = d - (pi.w + pj[u].w);
+                if (dv > 0.0f)
+                    continue;
+                e = fmaf(0.25f, dv * dv, e); // half the pair energy: weight 0.5 times E = dv^2 / 2
+                const float fod = dv * inv;
+                fx = fmaf(dx, fod, fx);
+                fy = fmaf(dy, fod, fy);
+                fz = fmaf(dz, fod, fz);
+            }
+            else
+            {
+                bool ok = inrow && r2 < lo2 && r2 > 1e-20f;
+                if (!ok && inrow && r2 < hi2)
+                    ok = exact_pair_test(pi, pj[u], p.c_steric, false);
+                ok = ok && !(r2 < 0.01f); // d < 0.1 A: the LJ forms give zero (steric.hpp:71-72)
+                const float fod = lj_pair<SM>(r2, ok, pi.w, fhi_i, pj[u], hj[u], 0.5f, e);
+                fx = fmaf(dx, fod, fx);
+                fy = fmaf(dy, fod, fy);
+                fz = fmaf(dz, fod, fz);
+            }
+        }
+    }
+}
+
+// Springs of slot s, lane t of T, in passes of kGatherU entries per lane (entries t + T u of the
+// ELL row, the same entries in the same order as spring_forces): the U entries' columns are read
+// first, then the U partner positions together.
+template <int T>
+__device__ __forceinline__ void spring_forces_batched(const Params &p, int s, int t, float4 pi,
+                                                      const float4 *__restrict__ pos, float &fx, float &fy, float &fz,
+                                                      float &e)
+{
+    constexpr int U = kGatherU;
+    const int deg = p.se_deg[s];
+    const size_t stride = static_cast<size_t>(p.npad);
+    for (int k0 = t; k0 < deg; k0 += T * U)
+    {
+        unsigned int c[U];
+        float kk[U], r0[U];
+        float4 pj[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+        {
+            const int k = k0 + u * T;
+            c[u] = kEntryInactive;
+            kk[u] = 0.0f;
+            r0[u] = 0.0f;
+            if (k < deg)
+            {
+                const size_t at = static_cast<size_t>(k) * stride + s;
+                c[u] = __ldg(&p.se_col[at]);
+                kk[u] = __ldg(&p.se_k[at]);
+                r0[u] = __ldg(&p.se_r0[at]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            pj[u] = (c[u] & kEntryInactive) ? pi : __ldg(&pos[c[u] & kSlotMask]);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+        {
+            if (c[u] & kEntryInactive)
+                continue;
+            const float dx = pj[u].x - pi.x, dy = pj[u].y - pi.y, dz = pj[u].z - pi.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const float inv = r2 > 0.0f ? rsqrt_nr(r2) : 0.0f;
+            const float len = r2 * inv;
+            const float dv = len - r0[u];
+            const float w = (c[u] & kEntryStatic) ? 1.0f : 0.5f;
+            e = fmaf(w * 0.5f * kk[u], dv * dv, e);
+            const float fod = kk[u] * dv * inv;
+            fx = fmaf(dx, fod, fx);
+            fy = fmaf(dy, fod, fy);
+            fz = fmaf(dz, fod, fz);
+        }
+    }
+}
+
 // Coulomb pairs of a charged slot, lane t of T (Particle.cpp:191-253, electrostatic.hpp:16-49).
 // With the distance-dependent dielectric eps = D r, E = K q q / (D r^2) and F = -dE/dr.
 template <int T>
@@ -633,6 +856,47 @@ __device__ __forceinline__ void field_forces(const Params &p, const float4 &pi, 
     }
 }
 
+// IMPALA for the double membrane with tube curvatures (imp.hpp:29-159, ForceField.cpp:62-85):
+// each membrane m, at signed offset o (upper +, lower -) with tube radius R = 1 / |curvature|
+// (1e6 A when flat) around an axis along y at z = o - sign R, sees the particle at depth d: its
+// z when flat, else its distance from the axis folded to the membrane's frame. The membrane adds
+// (-S T + A_lip S) C(|d - o|) to the energy and the opposite of that term's derivative along the
+// direction from the axis (z when flat) to the force.
+__device__ __forceinline__ void imp_double_membrane(const Params &p, const float4 &pi, float S, float T, float &fx,
+                                                    float &fz, float &e)
+{
+    const float gg = -S * T + kAlip * S;
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+    {
+        const float off = p.imp_off[m], c = p.imp_curv[m];
+        const float R = c == 0.0f ? 1000000.0f : fabsf(1.0f / c);
+        const float sg = c > 0.0f ? 1.0f : (c < 0.0f ? -1.0f : 0.0f);
+        const float axis = off - sg * R;
+        const float rx = pi.x, rz = pi.z - axis;
+        const float rn = sqrtf(rx * rx + rz * rz);
+        const float depth = sg == 0.0f ? pi.z : (pi.z > axis ? sg * rn : -sg * rn) + off - R;
+        const float u = depth - off;
+        const float ex = expf(p.imp_alpha * (fabsf(u) - p.imp_z0));
+        e = fmaf(p.imp_scale * gg, 0.5f - 1.0f / (1.0f + ex), e);
+        // dC/du = alpha sign(u) e / (1 + e)^2, written without overflow
+        float dcz = u != 0.0f ? p.imp_alpha / (ex + 2.0f + 1.0f / ex) : 0.0f;
+        if (u < 0.0f)
+            dcz = -dcz;
+        if (!isfinite(dcz))
+            dcz = 0.0f;
+        float dx = 0.0f, dz = 1.0f;
+        if (sg != 0.0f)
+        {
+            dx = rn > 1e-40f ? rx / rn : 0.0f;
+            dz = rn > 1e-40f ? rz / rn : 0.0f;
+        }
+        const float f = p.imp_scale * (gg * dcz * p.k_imp_f);
+        fx -= f * dx;
+        fz -= f * dz;
+    }
+}
+
 // Sum over the T consecutive lanes of a particle group (result in every lane of the group).
 template <int T> __device__ __forceinline__ float group_sum(float v)
 {
@@ -652,7 +916,7 @@ template <int T> __device__ __forceinline__ float group_sum(float v)
 // Coulomb rows walked by the whole warp. The batched kernel leaves both out (fewer live registers
 // under its 64-register budget: with them its spills grew and its step slowed by 7%); it walks
 // Coulomb rows with the particle's own lanes (the same pairs, summed in another order).
-template <int MODE, int SM, int T, bool SINGLE = true>
+template <int MODE, int SM, int T, bool SINGLE = true, bool LEAN = false>
 __device__ __forceinline__ int particle_step(const Params &p, const int s, const int t, const int send,
                                              const int sb, const int lb, const bool ext_on, float (&eacc)[6])
 {
@@ -676,7 +940,10 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
         if (p.spring_on)
         {
             float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
-            spring_forces<T>(p, s, t, pi, pos, sx, sy, sz, es);
+            if ((SINGLE && BS_GATHER) || (!SINGLE && BS_GATHER_BATCH))
+                spring_forces_batched<T>(p, s, t, pi, pos, sx, sy, sz, es);
+            else
+                spring_forces<T>(p, s, t, pi, pos, sx, sy, sz, es);
             const float kf = p.k_spring_f * p.spring_scale;
             fx = sx * kf;
             fy = sy * kf;
@@ -687,7 +954,16 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
         {
             float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
             const float fhi_i = p.fhi[lb][s];
-            if (p.pl16)
+            if (LEAN && p.lj_uniform && p.pl16)
+                steric_forces_batched<SM, T, true, true>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
+            else if ((SINGLE && BS_GATHER) || (!SINGLE && BS_GATHER_BATCH))
+            {
+                if (p.pl16)
+                    steric_forces_batched<SM, T, true>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
+                else
+                    steric_forces_batched<SM, T, false>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
+            }
+            else if (p.pl16)
                 steric_forces<SM, T, 0>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
             else
                 steric_forces<SM, T, 1>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
@@ -708,7 +984,7 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             fz = fmaf(sz, p.k_elec_f, fz);
             e[2] = es * p.k_elec_e;
         }
-        if (p.hydro_on && (fi & PF_HYDROPHOBIC))
+        if (!LEAN && p.hydro_on && (fi & PF_HYDROPHOBIC))
         {
             float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
             hydro_forces<T>(p, s, t, pi, p.hyd[lb][s], pos, p.hyd[lb], sx, sy, sz, es);
@@ -772,19 +1048,19 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             {
                 p.pos[sb ^ 1][s] = pi;
                 p.vel[sb ^ 1][s] = p.vel[sb][s];
-                if (p.pos_lo[0])
+                if (!LEAN && p.pos_lo[0])
                     p.pos_lo[sb ^ 1][s] = p.pos_lo[sb][s];
             }
             else
                 p.force_out[p.perm[lb][s]] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (p.probe_on)
+            if (!LEAN && p.probe_on)
                 p.probe_f[s] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         else
         {
             const float4 v = p.vel[sb][s];
             // ---- field grids (SpringNetwork.cpp:110-118) ----
-            if (SINGLE && (p.fg_on[0] || p.fg_on[1]))
+            if (SINGLE && !LEAN && (p.fg_on[0] || p.fg_on[1]))
                 field_forces(p, pi, p.chg[lb][s], p.fg_on[1] ? p.bur[lb][s] : 0.0f, fx, fy, fz, e[2]);
             // ---- viscosity (Particle.cpp:80-84) ----
             if (p.visc_on)
@@ -795,7 +1071,9 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             }
             const float4 ip = p.iprm[lb][s];
             // ---- IMPALA, flat membrane (imp.hpp:29-159, ForceField.cpp:62-88) ----
-            if (p.imp_on)
+            if (p.imp_on && p.imp_double)
+                imp_double_membrane(p, pi, ip.y, ip.z, fx, fz, e[4]);
+            else if (p.imp_on)
             {
                 const float ex = expf(p.imp_alpha * (fabsf(pi.z) - p.imp_z0));
                 const float cz = 0.5f - 1.0f / (1.0f + ex);
@@ -825,7 +1103,7 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
                 }
             }
             // ---- probe (SpringNetwork.cpp:156-182), after every other term ----
-            if (p.probe_on)
+            if (!LEAN && p.probe_on)
             {
                 const float4 prb = p.ctl->probe_pos;
                 float px = 0.f, py = 0.f, pz = 0.f;
@@ -839,7 +1117,7 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             {
                 p.force_out[p.perm[lb][s]] = make_float4(fx, fy, fz, 0.f);
             }
-            else if (fi & PF_RIGID)
+            else if (!LEAN && (fi & PF_RIGID))
             {
                 // a rigid particle's force goes to its body (RigidBody.cpp:567-580); the body
                 // kernel moves the particle, and its kinetic energy counts as zero
@@ -859,7 +1137,7 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
                 const float v2 = vx * vx + vy * vy + vz * vz;
                 e[5] = 0.5f * m * v2 * p.k_kin;
                 float nx, ny, nz;
-                if (p.pos_lo[0])
+                if (!LEAN && p.pos_lo[0])
                 {
                     // x += v dt in float-float: the increment's rounding error and the carried
                     // remainder are kept, so increments below half an ulp of x are not lost

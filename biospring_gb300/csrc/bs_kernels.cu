@@ -875,7 +875,7 @@ __global__ void __launch_bounds__(kPlWarps * 32, kPlMinBlocks) k_pairlist(Params
 // partial forces with shuffles, and the group's first lane adds the per-particle terms and
 // integrates. T > 1 gives the latency-bound gather loops T times more independent loads in
 // flight than one thread per particle would.
-template <int MODE, int SM, int T>
+template <int MODE, int SM, int T, bool LEAN>
 __global__ void __launch_bounds__(kStepKernelBlock, kStepMinBlocks) k_step(Params p)
 {
     pdl_enter();
@@ -885,7 +885,7 @@ __global__ void __launch_bounds__(kStepKernelBlock, kStepMinBlocks) k_step(Param
     const int sb = ctl->sbuf, lb = ctl->lbuf;
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     float e[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const int pend = particle_step<MODE, SM, T>(p, g / T, g % T, p.n, sb, lb, ctl->ext_pending != 0, e);
+    const int pend = particle_step<MODE, SM, T, true, LEAN>(p, g / T, g % T, p.n, sb, lb, ctl->ext_pending != 0, e);
     if (pend)
         atomicOr(&ctl->status_pending, pend);
     if (reduce_energies<6, kStepKernelBlock>(e, p.blk_energy, p.blk_cap, &ctl->done_step, ctl->energies))
@@ -1254,24 +1254,42 @@ int launch_rebuild(const Params &p, cudaStream_t st)
     return launched + 1;
 }
 
+// The lean step kernel leaves out, at compile time, the terms most systems do not use (pairwise
+// hydrophobic forces, field grids, the probe, rigid bodies, float-float positions): fewer live
+// registers, so the common kernel runs without register spills.
+static bool lean_step(const Params &p)
+{
+    return BS_LEAN && !(p.hydro_on || p.fg_on[0] || p.fg_on[1] || p.probe_on || p.nbody > 0 || p.pos_lo[0]);
+}
+
 template <int MODE, int SM>
 static void launch_step_lanes(const Params &p, cudaStream_t st)
 {
     const long long threads_per = p.step_lanes;
     const int nb = static_cast<int>((static_cast<long long>(p.n) * threads_per + kStepKernelBlock - 1) / kStepKernelBlock);
+    const bool lean = lean_step(p);
     switch (p.step_lanes)
     {
     case 2:
-        BS_STEP_LAUNCH(k_step<MODE, SM, 2>, nb, kStepKernelBlock, 0, st, p);
+        BS_STEP_LAUNCH(k_step<MODE, SM, 2, false>, nb, kStepKernelBlock, 0, st, p);
         break;
     case 8:
-        BS_STEP_LAUNCH(k_step<MODE, SM, 8>, nb, kStepKernelBlock, 0, st, p);
+        if (lean)
+            BS_STEP_LAUNCH(k_step<MODE, SM, 8, true>, nb, kStepKernelBlock, 0, st, p);
+        else
+            BS_STEP_LAUNCH(k_step<MODE, SM, 8, false>, nb, kStepKernelBlock, 0, st, p);
         break;
     case 16:
-        BS_STEP_LAUNCH(k_step<MODE, SM, 16>, nb, kStepKernelBlock, 0, st, p);
+        if (lean)
+            BS_STEP_LAUNCH(k_step<MODE, SM, 16, true>, nb, kStepKernelBlock, 0, st, p);
+        else
+            BS_STEP_LAUNCH(k_step<MODE, SM, 16, false>, nb, kStepKernelBlock, 0, st, p);
         break;
     default:
-        BS_STEP_LAUNCH(k_step<MODE, SM, 4>, nb, kStepKernelBlock, 0, st, p);
+        if (lean)
+            BS_STEP_LAUNCH(k_step<MODE, SM, 4, true>, nb, kStepKernelBlock, 0, st, p);
+        else
+            BS_STEP_LAUNCH(k_step<MODE, SM, 4, false>, nb, kStepKernelBlock, 0, st, p);
         break;
     }
 }

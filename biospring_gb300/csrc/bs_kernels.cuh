@@ -35,6 +35,20 @@ constexpr int kRebuildBlocking = ST_NONFINITE | ST_PAIR_CAPACITY | ST_CELL_CAPAC
 #ifndef BS_PDL
 #define BS_PDL 1
 #endif
+// Gathers in flight per lane in the step kernel's spring and steric loops: kGatherU entries are
+// read per pass and their partners loaded together (0: the entry-by-entry software-pipelined
+// loops). BS_GATHER_BATCH selects it for the persistent ensemble kernel.
+#ifndef BS_GATHER
+#define BS_GATHER 3
+#endif
+#ifndef BS_GATHER_BATCH
+#define BS_GATHER_BATCH 0
+#endif
+constexpr int kGatherU = 4;
+// the lean step kernel (BS_LEAN 0: always the full one)
+#ifndef BS_LEAN
+#define BS_LEAN 1
+#endif
 #ifndef BS_PDL_STEP
 #define BS_PDL_STEP 0
 #endif

@@ -125,6 +125,7 @@ SIGNATURES = {
     "bs_get_field_grid": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _f32p]),
     "bs_set_burying": (C.c_int, [C.c_void_p, _f32p]),
     "bs_set_charges": (C.c_int, [C.c_void_p, _f32p]),
+    "bs_set_membrane": (C.c_int, [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]),
     "bs_setup": (C.c_int, [C.c_void_p, C.POINTER(BsConfig)]),
     "bs_step": (C.c_int, [C.c_void_p, C.c_int32]),
     "bs_step_async": (C.c_int, [C.c_void_p, C.c_int32]),

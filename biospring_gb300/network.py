@@ -133,6 +133,13 @@ class SpringNetwork:
         b = _f32(burying)
         self._check(self._lib.bs_set_burying(self._h, ptr(b, C.c_float)), self._h)
 
+    def setMembrane(self, upper_offset: float = 0.0, lower_offset: float = 0.0, upper_curvature: float = 0.0,
+                    lower_curvature: float = 0.0):
+        """IMPALA double membrane (ForceField::setImpDoubleMembrane*): offsets in A, tube
+        curvatures in 1/A; all zero is the flat membrane."""
+        self._check(self._lib.bs_set_membrane(self._h, float(upper_offset), float(lower_offset),
+                                              float(upper_curvature), float(lower_curvature)), self._h)
+
     def setCharges(self, charge):
         """Replaces every particle's charge (caller order); Coulomb list membership follows at the
         next step."""

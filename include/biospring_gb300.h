@@ -230,6 +230,16 @@ int bs_get_field_grid(bs_sim *sim, int32_t which, int32_t shape[3], float *out);
  * weight of the density-grid force, caller order. */
 int bs_set_burying(bs_sim *sim, const float *burying);
 
+/* The IMPALA double membrane (replaces ForceField::setImpDoubleMembraneUpperMembOffset,
+ * ...LowerMembOffset, ...UpperMembTubeCurv, ...LowerMembTubeCurv, ForceField.h:100-110, which the
+ * MDDriver interactor sets, CustomData.cpp:61-107): the upper membrane centred at
+ * z = +upper_offset and the lower at z = -lower_offset (A), each bent into a tube along y of
+ * curvature 1/A (0: flat; the sign says which side the tube's axis lies on), energies and forces
+ * of energy/imp.hpp:29-159. All zero (the default) is the flat single membrane. Takes effect at
+ * the next step or force evaluation; valid at any time after bs_create. */
+int bs_set_membrane(bs_sim *sim, float upper_offset, float lower_offset, float upper_curvature,
+                    float lower_curvature);
+
 /* Replaces every particle's charge (ParticleProperty::setCharge, ParticleProperty.h:27, for the
  * whole array: float[n], caller order, finite), before or after bs_setup,
  * e.g. between steps of a charge fit driven by bs_adjoint's dL_dq. A particle whose charge becomes

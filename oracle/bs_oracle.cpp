@@ -116,6 +116,68 @@ struct FF
     float stericscale = 1, springscale = 1, impscale = 1, coulombscale = 1, hydroscale = 1, dielectric = 1;
     int dielectric_mode = BS_DIELECTRIC_CONSTANT;
     float imp_z0 = 15.75f, imp_alpha = 1.99f;
+    // double membrane: offsets of the upper and lower membranes and their tube curvatures
+    // (ForceField.h:23-25, 100-110); all zero for the flat membrane
+    float memb_uo = 0.0f, memb_lo = 0.0f, memb_uc = 0.0f, memb_lc = 0.0f;
+    bool flat() const { return memb_uo == 0.0f && memb_lo == 0.0f && memb_uc == 0.0f && memb_lc == 0.0f; }
+
+    // One membrane of the double membrane (imp.hpp:33-62, 100-129): the tube radius (1e6 A when
+    // flat), the curvature's sign, the z of the tube axis, the vector from that axis to the particle
+    // and the particle's z in the membrane's frame. `off` is the membrane's signed offset (+upper,
+    // -lower).
+    struct Side
+    {
+        float radius;
+        int sign;
+        V3 rel;
+        float depth;
+    };
+    static Side side(float x, float y, float z, float off, float curv)
+    {
+        Side d;
+        d.radius = curv == 0.0f ? 1000000.0f : std::abs(1 / curv);
+        d.sign = (curv > 0.0f) - (curv < 0.0f);
+        const V3 centre = {0.0f, y, off - d.sign * d.radius};
+        d.rel = sub(V3{x, y, z}, centre);
+        if (d.sign == 0)
+            d.depth = z;
+        else if (z > centre.z)
+            d.depth = d.sign * norm3(d.rel) + off - d.radius;
+        else
+            d.depth = -d.sign * norm3(d.rel) + off - d.radius;
+        return d;
+    }
+    // imp.hpp:29-77 with the double-membrane parameters set
+    float imp_energy_double(float x, float y, float z, float surface, float transfer) const
+    {
+        const Side u = side(x, y, z, memb_uo, memb_uc), l = side(x, y, z, -memb_lo, memb_lc);
+        const double cu = 0.5 - 1.0 / (1.0 + rexp(imp_alpha * (std::abs(u.depth - memb_uo) - imp_z0)));
+        const double cl = 0.5 - 1.0 / (1.0 + rexp(imp_alpha * (std::abs(l.depth + memb_lo) - imp_z0)));
+        const double hu = -surface * transfer * cu, hl = -surface * transfer * cl;
+        const double lu = C_ALIP * surface * cu, ll = C_ALIP * surface * cl;
+        return impscale * static_cast<float>(hu + lu + hl + ll);
+    }
+    // imp.hpp:88-159 with the double-membrane parameters set, ForceField.cpp:80-85
+    V3 imp_force_double(float x, float y, float z, float surface, float transfer) const
+    {
+        const Side u = side(x, y, z, memb_uo, memb_uc), l = side(x, y, z, -memb_lo, memb_lc);
+        auto expo = [&](float zz, float off) { return rexp(imp_alpha * (std::abs(zz + off) - imp_z0)); };
+        double du = (imp_alpha * (u.depth - memb_uo) * expo(u.depth, -memb_uo)) /
+                    (std::pow(expo(u.depth, -memb_uo) + 1, 2.0) * std::abs(u.depth - memb_uo));
+        double dl = (imp_alpha * (l.depth + memb_lo) * expo(l.depth, memb_lo)) /
+                    (std::pow(expo(l.depth, memb_lo) + 1, 2.0) * std::abs(l.depth + memb_lo));
+        if (std::isnan(du) || !std::isfinite(du))
+            du = 0.0;
+        if (std::isnan(dl) || !std::isfinite(dl))
+            dl = 0.0;
+        const V3 dir_u = normalize3(u.sign == 0 ? V3{0.0f, 0.0f, 1.0f} : u.rel);
+        const V3 dir_l = normalize3(l.sign == 0 ? V3{0.0f, 0.0f, 1.0f} : l.rel);
+        const double hu = -surface * transfer * du, hl = -surface * transfer * dl;
+        const double lu = C_ALIP * surface * du, ll = C_ALIP * surface * dl;
+        const V3 fu = mul(dir_u, static_cast<float>((hu + lu) * C_IMP_F));
+        const V3 fl = mul(dir_l, static_cast<float>((hl + ll) * C_IMP_F));
+        return mul(neg(add(fu, fl)), impscale);
+    }
 
     // spring.hpp:17-29 wrapped by ForceField.cpp:39-47
     float spring_energy(float d, float k, float r0) const
@@ -768,8 +830,16 @@ struct Sim
             }
             if (cfg.impala_enable)
             {
-                pe_imp[i] = ff.imp_energy(z[i], sasa[i], transfer[i]);
-                add_force(i, ff.imp_force(z[i], sasa[i], transfer[i]));
+                if (ff.flat())
+                {
+                    pe_imp[i] = ff.imp_energy(z[i], sasa[i], transfer[i]);
+                    add_force(i, ff.imp_force(z[i], sasa[i], transfer[i]));
+                }
+                else
+                {
+                    pe_imp[i] = ff.imp_energy_double(x[i], y[i], z[i], sasa[i], transfer[i]);
+                    add_force(i, ff.imp_force_double(x[i], y[i], z[i], sasa[i], transfer[i]));
+                }
             }
             if (cfg.hydrophobicity_enable && hydrophobic[i] && grid[2].active)
                 pair_term<BS_TERM_HYDROPHOBIC>(i, d_hydro[t]);
@@ -1194,6 +1264,16 @@ void bso_get_probe(void * h, float * out)
 
 void bso_destroy(void * h) { delete static_cast<Sim *>(h); }
 
+// The double membrane's offsets and tube curvatures (ForceField::setImpDoubleMembrane*).
+void bso_set_membrane(void * h, float upper_offset, float lower_offset, float upper_curv, float lower_curv)
+{
+    auto * s = static_cast<Sim *>(h);
+    s->ff.memb_uo = upper_offset;
+    s->ff.memb_lo = lower_offset;
+    s->ff.memb_uc = upper_curv;
+    s->ff.memb_lc = lower_curv;
+}
+
 // Body b owns ids[offsets[b] .. offsets[b+1]).
 int bso_set_rigid_bodies(void * h, int32_t nb, const int32_t * offsets, const int32_t * ids)
 {
@@ -1501,7 +1581,39 @@ int bso_eval_fp64(void * h, double * f_out, double * e_out)
             F[3 * i + 1] -= static_cast<double>(s->vy[i]) * c.viscosity_value;
             F[3 * i + 2] -= static_cast<double>(s->vz[i]) * c.viscosity_value;
         }
-        if (c.impala_enable)
+        if (c.impala_enable && !s->ff.flat())
+        {
+            // double membrane in FP64: each membrane's depth and direction from its tube axis
+            const double S = s->sasa[i], T = s->transfer[i];
+            const double a = static_cast<float>(c.impala_alpha), z0 = static_cast<float>(c.impala_z0);
+            const double offs[2] = {s->ff.memb_uo, -static_cast<double>(s->ff.memb_lo)};
+            const double curv[2] = {s->ff.memb_uc, s->ff.memb_lc};
+            for (int m = 0; m < 2; ++m)
+            {
+                const double R = curv[m] == 0.0 ? 1.0e6 : std::fabs(1.0 / curv[m]);
+                const int sg = (curv[m] > 0.0) - (curv[m] < 0.0);
+                const double cz_axis = offs[m] - sg * R;
+                const double rx = s->x[i], rz = s->z[i] - cz_axis, rn = std::sqrt(rx * rx + rz * rz);
+                const double depth = sg == 0 ? static_cast<double>(s->z[i])
+                                             : (s->z[i] > cz_axis ? sg * rn : -sg * rn) + offs[m] - R;
+                const double u = depth - offs[m];
+                const double ex = std::exp(a * (std::fabs(u) - z0));
+                E[BS_ENERGY_IMP] += s->ff.impscale * (-S * T + C_ALIP * S) * (0.5 - 1.0 / (1.0 + ex));
+                double dcz = a * u * ex / ((ex + 1) * (ex + 1) * std::fabs(u));
+                if (!std::isfinite(dcz))
+                    dcz = 0.0;
+                double dx = 0.0, dz = 1.0;
+                if (sg != 0)
+                {
+                    dx = rn > 0.0 ? rx / rn : 0.0;
+                    dz = rn > 0.0 ? rz / rn : 0.0;
+                }
+                const double f = s->ff.impscale * (-S * T + C_ALIP * S) * dcz * C_IMP_F;
+                F[3 * i] -= f * dx;
+                F[3 * i + 2] -= f * dz;
+            }
+        }
+        else if (c.impala_enable)
         {
             const double zz = s->z[i], S = s->sasa[i], T = s->transfer[i];
             const double a = static_cast<float>(c.impala_alpha), z0 = static_cast<float>(c.impala_z0);

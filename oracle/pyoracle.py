@@ -112,6 +112,7 @@ def _bind(lib, prefix: str, cfg_type):
         "get_cells": (C.c_int, [C.c_void_p, C.c_int32, _i64p]),
     }
     sig["get_probe"] = (None, [C.c_void_p, _f32p])
+    sig["set_membrane"] = (None, [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float])
     sig["set_burying"] = (None, [C.c_void_p, _f32p])
     if prefix == "bsref_":
         sig["get_field_grid"] = (None, [C.c_void_p, C.c_int32, _i32p, _f32p])
@@ -231,6 +232,10 @@ class _CpuSim:
         out = np.zeros(self.n, np.int64)
         self._fns["get_cells"](self.h, term, _p(out, C.c_int64))
         return out
+
+    def set_membrane(self, upper_offset=0.0, lower_offset=0.0, upper_curvature=0.0, lower_curvature=0.0):
+        self._fns["set_membrane"](self.h, float(upper_offset), float(lower_offset), float(upper_curvature),
+                                  float(lower_curvature))
 
     def set_burying(self, b):
         self._bur = np.ascontiguousarray(b, np.float32)

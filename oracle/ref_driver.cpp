@@ -158,6 +158,18 @@ void * bsref_create(const bs_config * cfg, int64_t n, const float * xyz, const f
     return h;
 }
 
+// The double membrane and its tube curvatures on the reference's force field, as the MDDriver
+// interactor sets them (src/interactor/mddriver/CustomData.cpp:61-107, ForceField.h:100-110).
+void bsref_set_membrane(void * hp, float upper_offset, float lower_offset, float upper_curv, float lower_curv)
+{
+    auto * h = static_cast<RefSim *>(hp);
+    biospring::forcefield::ForceField * ff = h->sn.getForceField();
+    ff->setImpDoubleMembraneUpperMembOffset(upper_offset);
+    ff->setImpDoubleMembraneLowerMembOffset(lower_offset);
+    ff->setImpDoubleMembraneUpperMembTubeCurv(upper_curv);
+    ff->setImpDoubleMembraneLowerMembTubeCurv(lower_curv);
+}
+
 // ParticleProperty::setBurying on every caller particle.
 void bsref_set_burying(void * hp, const float * b)
 {

@@ -26,6 +26,10 @@ Fixtures:
                   per-particle burying: the reference's grid cells (scalar, force vector), forces
                   and energies at the start, positions and energies after 1, 10 and 30 steps of a
                   fresh handle
+  membrane.npz    a 600-bead globule (displaced 0.2 A off its springs' rest lengths) with springs,
+                  IMPALA and viscosity under three double-membrane
+                  settings (offsets and tube curvatures of ForceField::setImpDoubleMembrane*):
+                  forces and energies at the start, positions and energies after 5 steps
   probe.npz       a charged 300-particle network with LJ 12-6 Amber and Coulomb, and the probe
                   particle (probe.*, SpringNetwork.cpp:156-182) steric and electrostatic on:
                   positions, probe state and energies after 1, 10 and 30 steps
@@ -180,6 +184,38 @@ def make_rigid() -> dict:
     return out
 
 
+# upper offset, lower offset, upper curvature, lower curvature
+MEMBRANES = np.array([[20.0, 20.0, 0.0, 0.0], [12.0, 14.0, 0.02, -0.015], [0.0, 25.0, 0.0, 0.03]], np.float32)
+
+
+def membrane_system() -> W.System:
+    s = W.membrane_globule(n=600, seed=6)
+    s.config.update(viscosity_value=0.5)
+    # off the springs' rest lengths, so that spring forces are real forces and not rounding residue
+    s.xyz = (s.xyz + np.random.default_rng(8).normal(0.0, 0.2, s.xyz.shape)).astype(np.float32)
+    return s
+
+
+def make_membrane() -> dict:
+    s = membrane_system()
+    out: dict = {"membranes": MEMBRANES}
+    system_arrays("in_", s, out)
+    for k, m in enumerate(MEMBRANES):
+        ref = po.Reference(s)
+        ref.set_membrane(*m)
+        ref.compute_forces()
+        out[f"force0_{k}"] = ref.forces()
+        out[f"energy0_{k}"] = ref.energies()
+        ref.close()
+        ref = po.Reference(s)
+        ref.set_membrane(*m)
+        ref.step(5)
+        out[f"pos5_{k}"] = ref.positions()
+        out[f"energy5_{k}"] = ref.energies()
+        ref.close()
+    return out
+
+
 def probe_system() -> W.System:
     s = W.ca_network(n=300, seed=5)
     rng = np.random.default_rng(3)
@@ -291,7 +327,7 @@ def main() -> None:
     if not po.build_reference():
         raise SystemExit("the reference sources are not present: cannot generate golden fixtures")
     makers = {"scans": None, "ca300": make_ca300, "rigid1": make_rigid, "nsearch": make_nsearch,
-              "probe": make_probe, "fields": make_fields}
+              "probe": make_probe, "fields": make_fields, "membrane": make_membrane}
     for mode in range(4):
         makers[f"mixed_m{mode}"] = (lambda m: (lambda: make_mixed(m)))(mode)
     wanted = sys.argv[1:] or list(makers)

@@ -2,8 +2,8 @@
 
 Bars (written in each test):
   * pair sets and cell ids: bit-exact;
-  * forces: ||F_gpu - F_ref||_2 / ||F_ref||_2 <= 1e-5 over the dynamic particles, and no
-    worse than 4x the reference arithmetic's own distance to FP64 when that is larger;
+  * forces: ||F_gpu - F_ref||_2 / ||F_ref||_2 <= 1e-5 over the dynamic particles (the reference
+    arithmetic's own distance to FP64 is printed beside it);
   * energies: relative 1e-5 (or the reference's own FP32 error vs FP64, whichever is larger);
   * trajectories: positions within 1e-4 A after tens of damped steps.
 """
@@ -24,12 +24,12 @@ ENERGY_TOL = 1e-5
 
 
 def force_tolerance(system, f_ref):
-    """1e-5, or 4x the FP32 reference's own relative distance to FP64 if that is larger."""
+    """The force bar, 1e-5, and the FP32 reference's own relative distance to FP64 (printed)."""
     orc = po.Oracle(system)
     f64, _ = orc.eval_fp64()
     own = rel_l2(f_ref, f64, dynamic_mask(system))
     orc.close()
-    return max(FORCE_TOL, 4.0 * own), own
+    return FORCE_TOL, own
 
 
 def energy_ok(e_gpu, e_ref, e64, k):
@@ -152,7 +152,7 @@ def test_uniform_lj_against_oracle_and_fp64():
     gerr = rel_l2(f_gpu, f64)
     print(f"uniform LJ 20k: gpu vs reference-arithmetic {err:.3e}, gpu vs FP64 {gerr:.3e}, "
           f"reference-arithmetic vs FP64 {own:.3e}")
-    assert err <= max(FORCE_TOL, 4 * own)
+    assert err <= FORCE_TOL
     for term in (0, 1):
         np.testing.assert_array_equal(net.getPairs(term), orc.pairs(term))
         np.testing.assert_array_equal(net.getCells(term), orc.cells(term))
@@ -174,7 +174,7 @@ def test_distance_dielectric_against_fp64():
     gerr = rel_l2(net.getForces(), f64)
     own = rel_l2(orc.forces(), f64)
     print(f"eps=4r: gpu vs FP64 {gerr:.3e}, FP32 restatement vs FP64 {own:.3e}")
-    assert gerr <= max(FORCE_TOL, 4 * own)
+    assert gerr <= FORCE_TOL
     e = np.array(list(net.energies().values()))
     assert rel_scalar(e[3], e64[3]) < 1e-5
 

@@ -159,3 +159,24 @@ def test_probe_particle():
         same(orc.positions(), g[f"pos_{mark}"])
         same(orc.probe(), g[f"probe_{mark}"])
         same(orc.energies(), g[f"energy_{mark}"])
+
+
+def test_double_membrane_matches_reference():
+    """IMPALA double membrane with tube curvatures (energy/imp.hpp:29-159 with the offsets and
+    curvatures of ForceField.h:23-25 set): forces and energies at the start and the state after 5
+    steps, under three settings."""
+    g = load_golden("membrane.npz")
+    s = system_from_golden(g)
+    for k, m in enumerate(g["membranes"]):
+        orc = po.Oracle(s)
+        orc.set_membrane(*m)
+        orc.compute_forces()
+        same(orc.forces(), g[f"force0_{k}"])
+        same(orc.energies(), g[f"energy0_{k}"])
+        orc.close()
+        orc = po.Oracle(s)
+        orc.set_membrane(*m)
+        orc.step(5)
+        same(orc.positions(), g[f"pos5_{k}"])
+        same(orc.energies(), g[f"energy5_{k}"])
+        orc.close()

@@ -318,8 +318,21 @@ class NcReader
         const bool rec = !v.dims.empty() && v.dims[0] == h_.record_dim;
         uint64_t per = 1; // values per record (or in total for a fixed-size variable)
         for (size_t k = rec ? 1 : 0; k < v.dims.size(); ++k)
-            per *= dim_size(v.dims[k]);
+        {
+            const uint64_t d = dim_size(v.dims[k]);
+            if (d != 0 && per > UINT64_MAX / d)
+            {
+                err = "array \"" + v.name + "\" declares more values than can be counted (damaged header)";
+                return false;
+            }
+            per *= d;
+        }
         const uint64_t nrec = rec ? h_.numrecs : 1;
+        if (per == 0 || nrec == 0)
+        {
+            out.clear(); // a zero-length dimension: nothing to read
+            return true;
+        }
         uint64_t recsize = 0;
         if (rec)
         {

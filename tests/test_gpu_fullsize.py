@@ -231,12 +231,17 @@ def test_membrane_20k_four_bodies(z0):
         x, xo = net.getPositions().astype(np.float64), orc.positions().astype(np.float64)
         dx = float(np.abs(x - xo).max())
         e, eo = _energies(net), orc.energies()
-        _, e64 = orc.eval_fp64()
-        print(f"Z0 {z0}, step {mark}: max |dx| {dx:.2e} A, energies {e} vs {eo} (FP64 {e64})")
         assert dx < 2e-5
-        for k in range(1, 6):
-            assert _energy_ok(e, eo, e64, k), (mark, k, e[k], eo[k], e64[k])
         assert rel_scalar(e[0], eo[0]) < 1e-4  # kinetic: FP32 sums of per-particle terms on both sides
+        # A step's energies are taken at the positions before its update; the potential energies
+        # are checked at the current state instead, against FP64 (the FP32 oracle's serial sum of
+        # some 2e5 spring energies is itself 1e-4 from the exact value here).
+        net.computeForces()
+        eg = _energies(net)
+        _, e64 = orc.eval_fp64()
+        print(f"Z0 {z0}, step {mark}: max |dx| {dx:.2e} A, energies {eg} vs FP64 {e64} (oracle's last step {eo})")
+        for k in range(1, 6):
+            assert abs(eg[k] - e64[k]) <= ENERGY_TOL * abs(e64[k]) + E_FLOOR, (mark, k, eg[k], e64[k])
     net.close()
     orc.close()
 

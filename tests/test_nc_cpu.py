@@ -185,3 +185,12 @@ def test_truncated_and_corrupted_files_fail_cleanly(tmp_path):
         except BsError:
             refused += 1
     assert refused >= len(data) // 7  # every cut file is refused
+
+
+def test_zero_length_arrays(tmp_path):
+    """A topology without springs: the spring arrays have a zero-length dimension and read as empty."""
+    from biospring_gb300 import capi
+    path = str(tmp_path / "nosprings.nc")
+    write_topology(path, n=20, m=0)
+    out = capi.read_nc(path)
+    assert out["ij"].shape == (0, 2) and out["r0"].shape == (0,) and out["xyz"].shape == (20, 3)

@@ -410,7 +410,7 @@ __device__ __forceinline__ void block_energy_partial(const float (&e)[NE], float
 // nominal number of steps of this launch: every live system runs until it has completed
 // ctl->nominal + chunk steps, unless its list goes stale first. chunk = 0 only lets systems that
 // fell behind catch up.
-template <int SM, int T>
+template <int SM, int T, bool LEAN>
 __global__ void __launch_bounds__(kBatchMaxBlock, 2) k_batch_run(Params p, int chunk)
 {
     cg::cluster_group cl = cg::this_cluster();
@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 2) k_batch_run(Params p, int c
             for (int g0 = 0; g0 < span; g0 += stride)
             {
                 const int g = g0 + me;
-                pend |= particle_step<MODE_STEP, SM, T, false>(p, n0 + g / T, g % T, n1, sb, lb, false, e);
+                pend |= particle_step<MODE_STEP, SM, T, false, LEAN>(p, n0 + g / T, g % T, n1, sb, lb, false, e);
             }
             if (pend)
             {
@@ -576,22 +576,28 @@ int launch_batch_pairlist(const Params &p, cudaStream_t st)
     return 1;
 }
 
-template <int SM, int T> static const void *batch_run_fn() { return reinterpret_cast<const void *>(&k_batch_run<SM, T>); }
+template <int SM, int T> static const void *batch_run_fn(bool lean)
+{
+    return lean ? reinterpret_cast<const void *>(&k_batch_run<SM, T, true>)
+                : reinterpret_cast<const void *>(&k_batch_run<SM, T, false>);
+}
 
-const void *batch_run_kernel(int steric_mode, int lanes)
+// The lean instance (no pairwise hydrophobic term, no float-float positions; ensembles have no
+// rigid bodies, probe or field grids) keeps fewer registers live under the kernel's 64.
+const void *batch_run_kernel(int steric_mode, int lanes, bool lean)
 {
 #define BS_RUN_CASE(SMV)                                                                                               \
     case SMV:                                                                                                          \
         switch (lanes)                                                                                                 \
         {                                                                                                              \
         case 1:                                                                                                        \
-            return batch_run_fn<SMV, 1>();                                                                             \
+            return batch_run_fn<SMV, 1>(lean);                                                                             \
         case 2:                                                                                                        \
-            return batch_run_fn<SMV, 2>();                                                                             \
+            return batch_run_fn<SMV, 2>(lean);                                                                             \
         case 8:                                                                                                        \
-            return batch_run_fn<SMV, 8>();                                                                             \
+            return batch_run_fn<SMV, 8>(lean);                                                                             \
         default:                                                                                                       \
-            return batch_run_fn<SMV, 4>();                                                                             \
+            return batch_run_fn<SMV, 4>(lean);                                                                             \
         }
     switch (steric_mode)
     {
@@ -607,7 +613,7 @@ const void *batch_run_kernel(int steric_mode, int lanes)
 
 cudaError_t launch_batch_run(const Params &p, const BatchShape &shape, int chunk, cudaStream_t st)
 {
-    const void *fn = batch_run_kernel(p.steric_mode, shape.lanes);
+    const void *fn = batch_run_kernel(p.steric_mode, shape.lanes, BS_LEAN && !p.hydro_on && !p.pos_lo[0]);
     if (!fn)
         return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg = {};
@@ -634,7 +640,7 @@ int launch_batch_finish(const Params &p, int chunk, cudaStream_t st)
 
 cudaError_t batch_max_clusters(const Params &p, const BatchShape &shape, int *out)
 {
-    const void *fn = batch_run_kernel(p.steric_mode, shape.lanes);
+    const void *fn = batch_run_kernel(p.steric_mode, shape.lanes, BS_LEAN && !p.hydro_on && !p.pos_lo[0]);
     if (!fn)
         return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg = {};

@@ -1090,9 +1090,12 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
     // ---- device allocation ----
     for (int b = 0; b < 2; ++b)
     {
-        BS_CUDA(s->dev.alloc(&p.pos[b], npad));
+        // one slot past the particles (a position far from everything, LJ factor zero), read by
+        // the step kernel for list entries past a row's end (no per-pair test of the row end)
+        BS_CUDA(s->dev.alloc(&p.pos[b], npad + 32));
         BS_CUDA(s->dev.alloc(&p.vel[b], npad));
-        BS_CUDA(s->dev.alloc(&p.fhi[b], npad));
+        BS_CUDA(s->dev.alloc(&p.fhi[b], npad + 32));
+        BS_CUDA(cudaMemsetAsync(p.fhi[b] + npad, 0, sizeof(float) * 32, s->stream));
         BS_CUDA(s->dev.alloc(&p.chg[b], npad));
         BS_CUDA(s->dev.alloc(&p.hyd[b], npad));
         BS_CUDA(s->dev.alloc(&p.flags[b], npad));
@@ -1239,6 +1242,11 @@ int bs_setup(bs_sim *s, const bs_config *cfg)
 
     // ---- uploads ----
     BS_CUDA(cudaMemcpyAsync(p.pos[0], pos0.data(), sizeof(float4) * npad, cudaMemcpyHostToDevice, s->stream));
+    {
+        static const float4 far_slot = make_float4(1.0e30f, 1.0e30f, 1.0e30f, 0.0f);
+        for (int b = 0; b < 2; ++b)
+            BS_CUDA(cudaMemcpyAsync(p.pos[b] + npad, &far_slot, sizeof(float4), cudaMemcpyHostToDevice, s->stream));
+    }
     BS_CUDA(cudaMemcpyAsync(p.vel[0], vel0.data(), sizeof(float4) * npad, cudaMemcpyHostToDevice, s->stream));
     BS_CUDA(cudaMemcpyAsync(p.fhi[0], fhi0.data(), sizeof(float) * npad, cudaMemcpyHostToDevice, s->stream));
     BS_CUDA(cudaMemcpyAsync(p.chg[0], chg0.data(), sizeof(float) * npad, cudaMemcpyHostToDevice, s->stream));

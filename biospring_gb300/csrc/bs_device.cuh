@@ -49,6 +49,19 @@ __device__ __forceinline__ float recip_nr(float x)
     return fmaf(r, fmaf(-x, r, 1.0f), r);
 }
 
+// 1/x for the LJ pair body: the refined reciprocal, or (BS_LJ_RCP_REFINE 0) the hardware
+// approximation alone.
+__device__ __forceinline__ float recip_lj(float x)
+{
+#if BS_LJ_RCP_REFINE
+    return recip_nr(x);
+#else
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#endif
+}
+
 // 1/sqrt(x): hardware approximation refined by one Newton-Raphson step for
 // f(r) = 1/r^2 - x, r1 = r0 (3 - x r0^2) / 2.
 __device__ __forceinline__ float rsqrt_nr(float x)
@@ -419,7 +432,7 @@ template <int SM>
 __device__ __forceinline__ float lj_pair(float r2, bool ok, float pw, float fhi_i, float4 pj, float hj, float w,
                                          float &e)
 {
-    const float inv2 = recip_nr(r2);
+    const float inv2 = recip_lj(r2);
     const float i6 = inv2 * inv2 * inv2;
     const float t6 = pw * pj.w * i6;
     float fod, de;
@@ -450,7 +463,7 @@ __device__ __forceinline__ float lj_pair(float r2, bool ok, float pw, float fhi_
 // load of the row (U offsets of 16 bits, or U slots), then issues the U partners' position and LJ
 // factor loads together before any of them is used, so U gathers are in flight per lane and a
 // warp waits for one round trip per U pairs instead of one per pair. Entries past the row's end
-// are replaced by the slot itself and rejected. Rows start on 16-byte boundaries (capacities are
+// read the slot past the particles (far from all of them) and fail the distance test. Rows start on 16-byte boundaries (capacities are
 // multiples of 8 entries), so the vector loads are aligned and never leave the row's capacity.
 template <int SM, int T, bool PL16, bool UF = false>
 __device__ __forceinline__ void steric_forces_batched(const Params &p, int s, int t, float4 pi, float fhi_i,
@@ -539,20 +552,22 @@ __device__ __forceinline__ void steric_forces_batched(const Params &p, int s, in
 #pragma unroll
         for (int u = 0; u < U; ++u)
         {
+            // past the row: a stale entry; the slot past the particles (far from every particle)
+            // is read instead, and its squared distance (infinite) rejects it below
             if ((BS_GATHER == 2 ? base + T * u : base + u) >= cnt)
-                j[u] = s; // past the row: a stale entry; the slot itself is read instead
+                j[u] = p.npad;
             pj[u] = __ldg(&pos[j[u]]);
             hj[u] = LJ ? (UF ? p.lj_F : __ldg(&fhi[j[u]])) : 0.0f; // one LJ type: no factor to gather
         }
+        unsigned int band = 0u; // LJ pairs of this pass within the guard band (BS_LJ_BAND_AFTER)
 #pragma unroll
         for (int u = 0; u < U; ++u)
         {
-            const bool inrow = (BS_GATHER == 2 ? base + T * u : base + u) < cnt;
             const float dx = pj[u].x - pi.x, dy = pj[u].y - pi.y, dz = pj[u].z - pi.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
             if (SM == BS_STERIC_LINEAR)
             {
-                if (!inrow || r2 >= hi2)
+                if (!(r2 < hi2))
                     continue;
                 if (!(r2 < lo2 && r2 > 1e-20f) && !exact_pair_test(pi, pj[u], p.c_steric, false))
                     continue;
@@ -569,11 +584,36 @@ __device__ __forceinline__ void steric_forces_batched(const Params &p, int s, in
             }
             else
             {
-                bool ok = inrow && r2 < lo2 && r2 > 1e-20f;
-                if (!ok && inrow && r2 < hi2)
+                // The FP32 squared distance decides outside the guard band [lo2, hi2); inside it
+                // (a few pairs per ten million) the exact test decides, either at once or
+                // (BS_LJ_BAND_AFTER) after the pass, which keeps the branch out of the pair body
+                // but the pass's partner data live longer. (Near-)coincident pairs need no exact
+                // test: below 0.1 A the LJ forms give zero (steric.hpp:71-72).
+#if BS_LJ_BAND_AFTER
+                const bool ok = r2 < lo2 && r2 >= 0.01f;
+                band |= (r2 >= lo2 && r2 < hi2) ? 1u << u : 0u;
+#else
+                bool ok = r2 < lo2;
+                if (!ok && r2 < hi2)
                     ok = exact_pair_test(pi, pj[u], p.c_steric, false);
-                ok = ok && !(r2 < 0.01f); // d < 0.1 A: the LJ forms give zero (steric.hpp:71-72)
+                ok = ok && r2 >= 0.01f;
+#endif
                 const float fod = lj_pair<SM>(r2, ok, pi.w, fhi_i, pj[u], hj[u], 0.5f, e);
+                fx = fmaf(dx, fod, fx);
+                fy = fmaf(dy, fod, fy);
+                fz = fmaf(dz, fod, fz);
+            }
+        }
+        if (BS_LJ_BAND_AFTER && SM != BS_STERIC_LINEAR && band)
+        {
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+            {
+                if (!((band >> u) & 1u) || !exact_pair_test(pi, pj[u], p.c_steric, false))
+                    continue;
+                const float dx = pj[u].x - pi.x, dy = pj[u].y - pi.y, dz = pj[u].z - pi.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                const float fod = lj_pair<SM>(r2, true, pi.w, fhi_i, pj[u], hj[u], 0.5f, e);
                 fx = fmaf(dx, fod, fx);
                 fy = fmaf(dy, fod, fy);
                 fz = fmaf(dz, fod, fz);
@@ -937,19 +977,6 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
     const bool active = s < send && !(fi & PF_STATIC);
     if (active)
     {
-        if (p.spring_on)
-        {
-            float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
-            if ((SINGLE && BS_GATHER) || (!SINGLE && BS_GATHER_BATCH))
-                spring_forces_batched<T>(p, s, t, pi, pos, sx, sy, sz, es);
-            else
-                spring_forces<T>(p, s, t, pi, pos, sx, sy, sz, es);
-            const float kf = p.k_spring_f * p.spring_scale;
-            fx = sx * kf;
-            fy = sy * kf;
-            fz = sz * kf;
-            e[0] = es * p.spring_scale;
-        }
         if (p.steric_on)
         {
             float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
@@ -974,6 +1001,20 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             fy = fmaf(sy, kf, fy);
             fz = fmaf(sz, kf, fz);
             e[1] = es * p.steric_scale;
+        }
+        // springs after the steric pairs: no spring sums are live across the steric loop
+        if (p.spring_on)
+        {
+            float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
+            if ((SINGLE && BS_GATHER) || (!SINGLE && BS_GATHER_BATCH))
+                spring_forces_batched<T>(p, s, t, pi, pos, sx, sy, sz, es);
+            else
+                spring_forces<T>(p, s, t, pi, pos, sx, sy, sz, es);
+            const float kf = p.k_spring_f * p.spring_scale;
+            fx = fmaf(sx, kf, fx);
+            fy = fmaf(sy, kf, fy);
+            fz = fmaf(sz, kf, fz);
+            e[0] = es * p.spring_scale;
         }
         if ((!SINGLE || !BS_COUL_WARP) && p.coulomb_on && (fi & PF_CHARGED))
         {

@@ -45,6 +45,13 @@ constexpr int kRebuildBlocking = ST_NONFINITE | ST_PAIR_CAPACITY | ST_CELL_CAPAC
 #define BS_GATHER_BATCH 0
 #endif
 constexpr int kGatherU = 4;
+// the LJ pair body refines the hardware reciprocal by one Newton step (0: the approximation alone)
+#ifndef BS_LJ_RCP_REFINE
+#define BS_LJ_RCP_REFINE 1
+#endif
+#ifndef BS_LJ_BAND_AFTER
+#define BS_LJ_BAND_AFTER 0
+#endif
 // the lean step kernel (BS_LEAN 0: always the full one)
 #ifndef BS_LEAN
 #define BS_LEAN 1

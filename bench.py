@@ -48,6 +48,9 @@ UNIT = "particle-steps/s"
 N_PARTICLES = 100_000
 BOX = 160.0
 REBUILD = 10
+# Verlet buffer of the device pair list: a particle drifts about 2e-4 A per 10-step period here,
+# so a 0.1 A skin keeps a margin of two orders of magnitude before a drift check forces a rebuild
+LIST_SKIN = 0.1
 STEP_BYTES_PER_PARTICLE_BASE = 84.0   # positions r+w 32, velocities r+w 32, parameters 16, row pointer 4
 SPRING_BYTES_PER_ENTRY = 12.0         # partner index + stiffness + rest length
 REBUILD_BYTES_PER_PARTICLE = 104.0    # key 4 + permutation 4 + gather/scatter of x, v, parameters 3 x 32
@@ -165,7 +168,7 @@ def replica_throughput(n: int, steps: int, slowest_ms: float, world: int) -> flo
 def make_workload(seed: int = 42, dielectric_mode: int = 1):
     from biospring_gb300 import workloads as W
     return W.uniform_lj(n=N_PARTICLES, box=BOX, seed=seed, dielectric_mode=dielectric_mode, rebuild_every=REBUILD,
-                        list_skin=0.5)
+                        list_skin=LIST_SKIN)
 
 
 def workload_config(system, world: int) -> dict:
@@ -174,7 +177,7 @@ def workload_config(system, world: int) -> dict:
     return {
         "workload": f"uniform_lj_100k: N={system.n}, cube {BOX:g} A, springs<5A (mean degree {dbar:.2f}), "
                     f"20% charged, Coulomb eps=4r 12 A, LJ 12-6 Amber 12 A, rebuild every {REBUILD} steps, "
-                    "list skin 0.5 A",
+                    f"list skin {LIST_SKIN:g} A",
         "global_batch": system.n * world,
         "parallelism": f"replicas{world}" if world > 1 else "single",
         "dielectric": DIELECTRIC_NOTE,

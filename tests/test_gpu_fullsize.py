@@ -94,8 +94,9 @@ def _sync_oracle(net, orc):
 
 @pytest.mark.parametrize("dielectric_mode", [0, 1], ids=["eps4", "eps4r"])
 def test_bench_system_100k(dielectric_mode):
+    import bench
     s = W.uniform_lj(n=100_000, box=160.0, seed=42, dielectric_mode=dielectric_mode, rebuild_every=10,
-                     list_skin=0.5)
+                     list_skin=bench.LIST_SKIN)
     net = gpu_network(s)
     orc = po.Oracle(s)
     _check_state(net, orc, f"100k eps mode {dielectric_mode}, first build")

@@ -605,7 +605,58 @@ def run_case(name: str) -> dict:
         loss, _, _ = net.adjoint(40, target, 20)
         net.close()
         return {"case": name, "loss": loss}
+    if name == "clusterpairs":
+        return cluster_pair_counts()
     raise SystemExit(f"unknown case {name}")
+
+
+def cluster_pair_counts(cluster_sizes=(4, 8)) -> dict:
+    """Pair evaluations a cluster-pair tile kernel would make on the 100k workload, against the
+    ordered pairs within the cutoff and the Verlet list entries the gather kernel reads (CPU,
+    scipy). Clusters are built as in cluster-pair MD codes: columns on an x-y grid whose cells
+    hold `c` particles per unit of the mean spacing, sorted by z, cut into groups of `c`; a cluster
+    pair is kept when the bounding boxes are closer than the list radius, and every slot of the
+    c x c tile is evaluated."""
+    from scipy.spatial import cKDTree
+    system = make_workload()
+    x = system.xyz.astype(np.float64)
+    n = x.shape[0]
+    rc = float(system.config["steric_cutoff"])
+    rl = rc + LIST_SKIN
+    tree = cKDTree(x)
+    useful = int(tree.count_neighbors(tree, rc)) - n
+    listed = int(tree.count_neighbors(tree, rl)) - n
+    lo, hi = x.min(0), x.max(0)
+    dens = n / float(np.prod(hi - lo))
+    out = {"case": "clusterpairs", "ordered_pairs_within_cutoff": useful, "verlet_entries_upper": listed}
+    for c in cluster_sizes:
+        a = (c / dens) ** (1.0 / 3.0)
+        ncol = np.maximum(1, np.floor((hi[:2] - lo[:2]) / a).astype(int))
+        cx = np.minimum(((x[:, 0] - lo[0]) / (hi[0] - lo[0]) * ncol[0]).astype(int), ncol[0] - 1)
+        cy = np.minimum(((x[:, 1] - lo[1]) / (hi[1] - lo[1]) * ncol[1]).astype(int), ncol[1] - 1)
+        col = cx * ncol[1] + cy
+        order = np.lexsort((x[:, 2], col))
+        starts = np.r_[0, np.flatnonzero(np.diff(col[order])) + 1]
+        ends = np.r_[starts[1:], n]
+        cid = np.empty(n, np.int64)
+        nc = 0
+        for b, e in zip(starts, ends):
+            k = np.arange(e - b) // c
+            cid[order[b:e]] = nc + k
+            nc += int(k[-1]) + 1
+        bmin = np.full((nc, 3), np.inf)
+        bmax = np.full((nc, 3), -np.inf)
+        np.minimum.at(bmin, cid, x)
+        np.maximum.at(bmax, cid, x)
+        cen, half = (bmin + bmax) / 2, (bmax - bmin) / 2
+        reach = rl + 2.0 * float(np.linalg.norm(half, axis=1).max())
+        pr = cKDTree(cen).query_pairs(reach, output_type="ndarray")
+        pr = np.vstack([pr, pr[:, ::-1], np.c_[np.arange(nc), np.arange(nc)]])
+        gap = np.maximum(0.0, np.maximum(bmin[pr[:, 0]] - bmax[pr[:, 1]], bmin[pr[:, 1]] - bmax[pr[:, 0]]))
+        kept = int(((gap * gap).sum(1) < rl * rl).sum())
+        out[f"clusters_{c}"] = {"clusters": nc, "cluster_pairs": kept, "evaluations": kept * c * c,
+                                "evaluations_per_useful_pair": kept * c * c / useful}
+    return out
 
 
 def _oracle_steps_per_s(system, steps: int, warmup: int) -> tuple[float, float]:
@@ -685,7 +736,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and adjoint figures")
-    ap.add_argument("--case", choices=["step100k", "batch64", "adjoint10k"],
+    ap.add_argument("--case", choices=["step100k", "batch64", "adjoint10k", "clusterpairs"],
                     help="run one small profiling driver instead of the benchmark")
     args = ap.parse_args()
     if args.case:

@@ -58,7 +58,7 @@ CTL_BYTES = 288                       # device control block (status, step count
 # DRAM bytes (read + write) of one k_step launch on this workload after an L2 flush, from one ncu
 # capture of dram__bytes_read.sum + dram__bytes_write.sum, and the digest of the step kernel's
 # sources that capture ran on: when the sources have changed since, the line marks the figure stale.
-STEP_KERNEL_TRAFFIC = {"bytes": 78.07e6 + 2.34e6, "sources_sha": "unrecorded", "captured": "2026-12-03"}
+STEP_KERNEL_TRAFFIC = {"bytes": 69.889024e6 + 1.767936e6, "sources_sha": "867c948f0d9817e2", "captured": "2026-12-04"}
 STEP_KERNEL_SOURCES = ("biospring_gb300/csrc/bs_device.cuh", "biospring_gb300/csrc/bs_kernels.cu",
                        "biospring_gb300/csrc/bs_kernels.cuh", "biospring_gb300/csrc/bs_common.cuh")
 DIELECTRIC_NOTE = ("Coulomb eps = 4r (distance-dependent), as the 100k configuration states; the reference's "
@@ -324,6 +324,10 @@ def run_native(args) -> dict:
             "kernel_ms": kernel_s * 1e3,
             "flops_per_step": alg["step_flops"],
             "fp32_tflops": alg["step_flops"] / kernel_s / 1e12,
+            # no FP32 peak is measured on this part: the nominal one (152 SMs x 128 lanes x 2 flops
+            # at the maximum SM clock) gives context only
+            "fp32_frac_of_nominal": alg["step_flops"] / kernel_s / (152 * 128 * 2 * 2.07e9),
+            "dram_frac": STEP_KERNEL_TRAFFIC["bytes"] / kernel_s / 1e9 / pk["hbm_gbs"],
         },
         "warm_continuous": {"value": system.n * 10 * REBUILD / (warm_ms * 1e-3), "unit": UNIT,
                             "ms_per_step": warm_ms / (10 * REBUILD)},

@@ -468,20 +468,23 @@ __device__ __forceinline__ float lj_pair(float r2, bool ok, float pw, float fhi_
 template <int SM, int T, bool PL16, bool UF = false>
 __device__ __forceinline__ void steric_forces_batched(const Params &p, int s, int t, float4 pi, float fhi_i,
                                                       const float4 *__restrict__ pos, const float *__restrict__ fhi,
-                                                      float &fx, float &fy, float &fz, float &e)
+                                                      float &fx, float &fy, float &fz, float &e, int cnt_in = -1,
+                                                      uint2 w16_in = make_uint2(0u, 0u))
 {
     constexpr int U = kGatherU;
     static_assert(U == 4, "one 8-byte (16-bit mode) or 16-byte (32-bit mode) load per pass");
     const PairList &L = p.pl[0];
-    const int cnt = L.cnt[s];
+    // cnt_in >= 0: the caller has already read the row's count and (16-bit rows) the lane's first
+    // four entries
+    const int cnt = cnt_in >= 0 ? cnt_in : L.cnt[s];
     const size_t row = static_cast<size_t>(s) * L.cap;
     const float lo2 = p.lo2_s, hi2 = p.hi2_s;
     constexpr bool LJ = SM != BS_STERIC_LINEAR;
     // BS_GATHER 3: the next pass's entries are loaded before this pass's partners, so the entry
     // load of a pass overlaps the previous pass instead of preceding its partner loads.
-    uint2 w16n = make_uint2(0u, 0u);
+    uint2 w16n = w16_in;
     uint4 w32n = make_uint4(0u, 0u, 0u, 0u);
-    if (BS_GATHER == 3 && U * t < cnt)
+    if (BS_GATHER == 3 && U * t < cnt && !(PL16 && cnt_in >= 0))
     {
         if (PL16)
             w16n = __ldg(reinterpret_cast<const uint2 *>(reinterpret_cast<const short *>(L.idx) + row + U * t));
@@ -969,10 +972,24 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
     float fx = 0.f, fy = 0.f, fz = 0.f;
     unsigned int fi = PF_STATIC;
     float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+    // BS_HOIST: the lean single-system step reads the steric row's count and the lane's first
+    // entries with the particle itself, so the row's first partner loads wait for one round trip
+    // fewer (the entries lie inside the row's capacity whatever the count)
+    constexpr bool kHoist = BS_HOIST && LEAN && SINGLE;
+    int cnt0 = -1;
+    uint2 w0 = make_uint2(0u, 0u);
     if (s < send)
     {
         pi = pos[s];
         fi = p.flags[lb][s];
+        if (kHoist && p.steric_on && p.lj_uniform && p.pl16)
+        {
+            const PairList &L = p.pl[0];
+            cnt0 = L.cnt[s];
+            if (kGatherU * t < L.cap)
+                w0 = __ldg(reinterpret_cast<const uint2 *>(reinterpret_cast<const short *>(L.idx) +
+                                                         static_cast<size_t>(s) * L.cap + kGatherU * t));
+        }
     }
     const bool active = s < send && !(fi & PF_STATIC);
     if (active)
@@ -982,7 +999,7 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
             float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
             const float fhi_i = p.fhi[lb][s];
             if (LEAN && p.lj_uniform && p.pl16)
-                steric_forces_batched<SM, T, true, true>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
+                steric_forces_batched<SM, T, true, true>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es, cnt0, w0);
             else if ((SINGLE && BS_GATHER) || (!SINGLE && BS_GATHER_BATCH))
             {
                 if (p.pl16)

@@ -52,6 +52,9 @@ constexpr int kGatherU = 4;
 #ifndef BS_LJ_BAND_AFTER
 #define BS_LJ_BAND_AFTER 0
 #endif
+#ifndef BS_HOIST
+#define BS_HOIST 1
+#endif
 // the lean step kernel (BS_LEAN 0: always the full one)
 #ifndef BS_LEAN
 #define BS_LEAN 1

@@ -609,6 +609,37 @@ def run_case(name: str) -> dict:
         loss, _, _ = net.adjoint(40, target, 20)
         net.close()
         return {"case": name, "loss": loss}
+    if name == "batch512":
+        # the bench's ensemble (512 systems, 2.1M particles): rebuild chain and whole periods
+        ens = W.ensemble(W.ensemble_sizes(), seed=2024)
+        net = SpringNetwork()
+        net.addParticles(xyz=ens.xyz)
+        net.addSprings(ens.ij, ens.r0, ens.k)
+        net.setSystems(ens.meta["offsets"])
+        net.setup(ens.bs_config())
+        net.computeStep(3 * REBUILD)
+        shape = net.batchAutotune()
+        net.computeStep(3 * REBUILD)
+        net.synchronize()
+        stream = torch.cuda.ExternalStream(net.stream())
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        with torch.cuda.stream(stream):
+            e[0].record(stream)
+            for _ in range(3):
+                net.launchPhase(0)
+            e[1].record(stream)
+        net.synchronize()
+        net.computeStep(REBUILD)  # back to a whole period after the extra rebuilds
+        net.synchronize()
+        e[2].record(stream)
+        net.computeStepAsync(5 * REBUILD)
+        e[3].record(stream)
+        net.synchronize()
+        torch.cuda.synchronize()
+        out = {"case": name, "particles": int(ens.n), "shape": list(shape),
+               "rebuild_ms": e[0].elapsed_time(e[1]) / 3, "period_ms": e[2].elapsed_time(e[3]) / 5}
+        net.close()
+        return out
     if name == "clusterpairs":
         return cluster_pair_counts()
     raise SystemExit(f"unknown case {name}")
@@ -740,7 +771,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and adjoint figures")
-    ap.add_argument("--case", choices=["step100k", "batch64", "adjoint10k", "clusterpairs"],
+    ap.add_argument("--case", choices=["step100k", "batch64", "batch512", "adjoint10k", "clusterpairs"],
                     help="run one small profiling driver instead of the benchmark")
     args = ap.parse_args()
     if args.case:

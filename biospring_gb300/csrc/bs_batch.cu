@@ -198,14 +198,18 @@ __global__ void __launch_bounds__(1024) k_batch_cell_scan(Params p)
 // Typed pair lists, one warp per home particle: the rules of the cell-block build (every pair
 // within the list radius of its term, the slot itself and spring partners excluded, static
 // partners of the steric term apart); the warp walks the (2 kSparseDiv + 1)^2 contiguous x-runs of
-// the neighbour cells, 32 candidates per pass, and a ballot appends the accepted ones to the row
-// in ascending slot order. Used for batched ensembles (BATCH: each system's own grid) and for
+// the neighbour cells packed into one sequence of full 32-candidate windows, and a ballot appends
+// the accepted ones to the row in run order and ascending slot order within a run. Spring partners
+// sit in registers, are located once in the candidate sequence and are excluded by a per-window
+// lane mask. Used for batched ensembles (BATCH: each system's own grid) and for
 // sparse single systems (a few particles per cell or fewer), where one block per group of cells
 // would mostly schedule empty blocks.
 template <bool PL16, bool BATCH>
 __global__ void __launch_bounds__(kBatchPlWarps * 32) k_batch_pairlist(Params p)
 {
-    __shared__ int sh_part[kBatchPlWarps][kPlMaxDeg];
+    constexpr int kSpan = 2 * kSparseDiv + 1;
+    static_assert(kSpan * kSpan <= 32, "one lane per x-run");
+    __shared__ int sh_cr[kBatchPlWarps][2 * kSpan * kSpan]; // per warp: the non-empty runs' first slot and first k
     Ctl *ctl = p.ctl;
     if (status_of(ctl) & kRebuildBlocking)
         return;
@@ -218,8 +222,6 @@ __global__ void __launch_bounds__(kBatchPlWarps * 32) k_batch_pairlist(Params p)
     const int cap0 = p.pl[0].cap, cap1 = p.pl[1].cap, cap2 = p.pl[2].cap, cap3 = p.pl[3].cap;
     const size_t stride = static_cast<size_t>(p.npad);
     const unsigned int below = (1u << lane) - 1u;
-    int *part = sh_part[wid];
-    constexpr int kSpan = 2 * kSparseDiv + 1;
     for (int i = blockIdx.x * kBatchPlWarps + wid; i < p.n; i += gridDim.x * kBatchPlWarps)
     {
         const unsigned int fi = fl[i];
@@ -249,109 +251,161 @@ __global__ void __launch_bounds__(kBatchPlWarps * 32) k_batch_pairlist(Params p)
             }
             const int lc = p.cell_of[i] - cbase;
             const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
-            // spring partners of i, sorted ascending in shared memory (rank sort across the warp)
+            // spring partners of i in registers: lane m holds partners m and m + 32 (slots, -1 for
+            // none); a home with more than 64 compares every candidate with its ELL row
             const int deg = p.spring_on ? p.se_deg[i] : 0;
-            const bool small = deg <= kPlMaxDeg;
-            __syncwarp();
-            if (small)
-                for (int k0 = 0; k0 < deg; k0 += 32)
-                {
-                    const int k = k0 + lane;
-                    const int v = k < deg ? static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask) : 0;
-                    int rank = 0;
-                    for (int m = 0; m < deg; ++m)
-                    {
-                        const int w = static_cast<int>(p.se_col[static_cast<size_t>(m) * stride + i] & kSlotMask);
-                        rank += (w < v) || (w == v && m < k);
-                    }
-                    if (k < deg)
-                        part[rank] = v;
-                }
-            __syncwarp();
-            int bp = 0;
+            const bool small = deg <= 64;
+            const int ps0 = small && lane < deg ? static_cast<int>(p.se_col[static_cast<size_t>(lane) * stride + i] & kSlotMask) : -1;
+            const int ps1 =
+                small && lane + 32 < deg ? static_cast<int>(p.se_col[static_cast<size_t>(lane + 32) * stride + i] & kSlotMask) : -1;
             short *row0s = reinterpret_cast<short *>(p.pl[0].idx) + static_cast<size_t>(i) * cap0;
             unsigned int *row0 = p.pl[0].idx + static_cast<size_t>(i) * cap0;
             unsigned int *row1 = p.pl[1].idx + static_cast<size_t>(i) * cap1;
             unsigned int *row2 = p.pl[2].idx + static_cast<size_t>(i) * cap2;
             unsigned int *row3 = p.pl[3].idx + static_cast<size_t>(i) * cap3;
-            for (int r = 0; r < kSpan * kSpan; ++r)
+            // lane r < kSpan^2 holds run r (cell offsets -kSparseDiv + r % kSpan in y and
+            // -kSparseDiv + r / kSpan in z): the contiguous slots of its 2 kSparseDiv + 1 cells in x
+            int lo_r = 0, cnt_r = 0;
+            if (lane < kSpan * kSpan)
             {
-                const int y = cy + r % kSpan - kSparseDiv;
-                const int z = cz + r / kSpan - kSparseDiv;
-                if (y < 0 || y >= ny || z < 0 || z >= nz)
-                    continue;
-                const int rowc = cbase + (z * ny + y) * nx;
-                const int j0 = p.cell_start[rowc + max(cx - kSparseDiv, 0)];
-                const int j1 = p.cell_start[rowc + min(cx + kSparseDiv, nx - 1) + 1];
-                for (int jb = j0; jb < j1; jb += 32)
+                const int y = cy + lane % kSpan - kSparseDiv;
+                const int z = cz + lane / kSpan - kSparseDiv;
+                if (y >= 0 && y < ny && z >= 0 && z < nz)
                 {
-                    const int j = jb + lane;
-                    const bool jv = j < j1;
-                    const int jc = jv ? j : j1 - 1;
-                    const float4 pj = pos[jc];
-                    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                    const float r2 = dx * dx + dy * dy + dz * dz;
-                    bool in = jv && r2 < r2max && j != i;
-                    if (deg)
+                    const int rowc = cbase + (z * ny + y) * nx;
+                    lo_r = p.cell_start[rowc + max(cx - kSparseDiv, 0)];
+                    cnt_r = p.cell_start[rowc + min(cx + kSparseDiv, nx - 1) + 1] - lo_r;
+                }
+            }
+            // The runs are walked as one sequence of candidates (k = 0 .. total-1, in run order,
+            // hence ascending slots within each run and rows in the order of the run-by-run walk),
+            // so that every window but the last is full. Lane c holds the c-th non-empty run: its
+            // first slot and its first k.
+            const unsigned int ne = __ballot_sync(0xffffffffu, cnt_r > 0);
+            int incl = cnt_r;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1)
+            {
+                const int v = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d)
+                    incl += v;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            const int nr = __popc(ne);
+            int *cr = sh_cr[wid];
+            __syncwarp();
+            if (cnt_r > 0)
+            {
+                const int c = __popc(ne & below);
+                cr[2 * c] = lo_r;
+                cr[2 * c + 1] = incl - cnt_r;
+            }
+            __syncwarp();
+            const int lo_c = lane < nr ? cr[2 * lane] : 0;
+            const int pre_c = lane < nr ? cr[2 * lane + 1] : total;
+            const int nxt = __shfl_down_sync(0xffffffffu, pre_c, 1);
+            const int end_c = lane + 1 < nr ? nxt : total;
+            // each spring partner's index in the candidate sequence (-1: not a candidate): the
+            // last run whose first slot is <= the partner's, by a binary search over the lanes'
+            // runs (runs are contiguous slot ranges)
+            int pk0 = -1, pk1 = -1;
+            if (deg > 0 && small && total > 0)
+            {
+                const int s_c = lane < nr ? lo_c : INT_MAX;
+                const int n_c = end_c - pre_c;
+                auto locate = [&](const int ps) {
+                    int at = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1)
                     {
-                        if (small)
-                        {
-                            while (bp < deg && part[bp] < jb)
-                                ++bp;
-                            for (int k = bp; k < deg && part[k] < jb + 32; ++k)
-                                in = in && part[k] != j;
-                        }
-                        else
-                            for (int k = 0; k < deg; ++k)
-                                in = in && static_cast<int>(p.se_col[static_cast<size_t>(k) * stride + i] & kSlotMask) != j;
+                        const int v = __shfl_sync(0xffffffffu, s_c, (at + step) & 31);
+                        if (at + step < nr && v <= ps)
+                            at += step;
                     }
-                    const unsigned int fj = need_fj ? fl[jc] : 0u;
-                    const bool st = (fj & PF_STATIC) != 0;
-                    if (on0)
+                    const int s0 = __shfl_sync(0xffffffffu, s_c, at);
+                    const int n0 = __shfl_sync(0xffffffffu, n_c, at);
+                    const int k0 = __shfl_sync(0xffffffffu, pre_c, at);
+                    return ps >= s0 && ps < s0 + n0 ? k0 + (ps - s0) : -1;
+                };
+                pk0 = locate(ps0);
+                if (deg > 32)
+                    pk1 = locate(ps1);
+            }
+            for (int wb = 0; wb < total; wb += 32)
+            {
+                const int k = wb + lane;
+                const int rr = __popc(__ballot_sync(0xffffffffu, lane < nr && end_c <= wb));
+                const int t = pre_c - wb;
+                const unsigned int starts =
+                    __reduce_or_sync(0xffffffffu, (lane < nr && t > 0 && t < 32) ? (1u << t) : 0u);
+                const int rk = min(rr + __popc(starts & ((2u << lane) - 1u)), nr - 1);
+                const int lo = __shfl_sync(0xffffffffu, lo_c, rk);
+                const int pre = __shfl_sync(0xffffffffu, pre_c, rk);
+                const bool jv = k < total;
+                const int j = jv ? lo + (k - pre) : lo;
+                // the lanes whose candidate is a spring partner, OR-ed over the warp
+                unsigned int bonded = 0u;
+                if (deg > 0 && small)
+                {
+                    const int t0 = pk0 < 0 ? -1 : pk0 - wb, t1 = pk1 < 0 ? -1 : pk1 - wb;
+                    unsigned int bb = t0 >= 0 && t0 < 32 ? 1u << t0 : 0u;
+                    if (t1 >= 0 && t1 < 32)
+                        bb |= 1u << t1;
+                    bonded = __reduce_or_sync(0xffffffffu, bb);
+                }
+                const float4 pj = pos[j];
+                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                bool in = jv && r2 < r2max && j != i && !((bonded >> lane) & 1u);
+                if (!small)
+                    for (int q = 0; q < deg; ++q)
+                        in = in && static_cast<int>(p.se_col[static_cast<size_t>(q) * stride + i] & kSlotMask) != j;
+                const unsigned int fj = need_fj ? fl[j] : 0u;
+                const bool st = (fj & PF_STATIC) != 0;
+                if (on0)
+                {
+                    const bool a0 = in && !st && r2 < r2_0;
+                    const unsigned int m0 = __ballot_sync(0xffffffffu, a0);
+                    if (a0)
                     {
-                        const bool a0 = in && !st && r2 < r2_0;
-                        const unsigned int m0 = __ballot_sync(0xffffffffu, a0);
-                        if (a0)
+                        const int at = cnt0 + __popc(m0 & below);
+                        if (at < cap0)
                         {
-                            const int at = cnt0 + __popc(m0 & below);
-                            if (at < cap0)
+                            if (PL16)
                             {
-                                if (PL16)
-                                {
-                                    const int off = j - i;
-                                    wide = wide || off < -32768 || off > 32767;
-                                    row0s[at] = static_cast<short>(off);
-                                }
-                                else
-                                    row0[at] = static_cast<unsigned int>(j);
+                                const int off = j - i;
+                                wide = wide || off < -32768 || off > 32767;
+                                row0s[at] = static_cast<short>(off);
                             }
-                        }
-                        cnt0 += __popc(m0);
-                        if (l3)
-                        {
-                            const bool a3 = in && st && r2 < r2_0;
-                            const unsigned int m3 = __ballot_sync(0xffffffffu, a3);
-                            if (a3 && cnt3 + __popc(m3 & below) < cap3)
-                                row3[cnt3 + __popc(m3 & below)] = static_cast<unsigned int>(j) | kEntryStatic;
-                            cnt3 += __popc(m3);
+                            else
+                                row0[at] = static_cast<unsigned int>(j);
                         }
                     }
-                    if (on1)
+                    cnt0 += __popc(m0);
+                    if (l3)
                     {
-                        const bool a1 = in && ((fj & PF_CHARGED) || p.coul_all) && r2 < r2_1;
-                        const unsigned int m1 = __ballot_sync(0xffffffffu, a1);
-                        if (a1 && cnt1 + __popc(m1 & below) < cap1)
-                            row1[cnt1 + __popc(m1 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
-                        cnt1 += __popc(m1);
+                        const bool a3 = in && st && r2 < r2_0;
+                        const unsigned int m3 = __ballot_sync(0xffffffffu, a3);
+                        if (a3 && cnt3 + __popc(m3 & below) < cap3)
+                            row3[cnt3 + __popc(m3 & below)] = static_cast<unsigned int>(j) | kEntryStatic;
+                        cnt3 += __popc(m3);
                     }
-                    if (on2)
-                    {
-                        const bool a2 = in && (fj & PF_HYDROPHOBIC) && r2 < r2_2;
-                        const unsigned int m2 = __ballot_sync(0xffffffffu, a2);
-                        if (a2 && cnt2 + __popc(m2 & below) < cap2)
-                            row2[cnt2 + __popc(m2 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
-                        cnt2 += __popc(m2);
-                    }
+                }
+                if (on1)
+                {
+                    const bool a1 = in && ((fj & PF_CHARGED) || p.coul_all) && r2 < r2_1;
+                    const unsigned int m1 = __ballot_sync(0xffffffffu, a1);
+                    if (a1 && cnt1 + __popc(m1 & below) < cap1)
+                        row1[cnt1 + __popc(m1 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
+                    cnt1 += __popc(m1);
+                }
+                if (on2)
+                {
+                    const bool a2 = in && (fj & PF_HYDROPHOBIC) && r2 < r2_2;
+                    const unsigned int m2 = __ballot_sync(0xffffffffu, a2);
+                    if (a2 && cnt2 + __popc(m2 & below) < cap2)
+                        row2[cnt2 + __popc(m2 & below)] = static_cast<unsigned int>(j) | (st ? kEntryStatic : 0u);
+                    cnt2 += __popc(m2);
                 }
             }
         }

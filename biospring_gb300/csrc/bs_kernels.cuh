@@ -85,7 +85,6 @@ constexpr int kPlStage = BS_PL_STAGE; // candidate positions staged in shared me
 constexpr int kPlMinBlocks = 4;       // resident list-build blocks per SM (the stage allows 4)
 constexpr int kPlBatch = 16;         // home particles per warp
 constexpr int kPlBatchesPerCell = 4; // warps per cell (a cell with more than 64 particles loops)
-constexpr int kPlMaxDeg = 48;        // spring partners kept in shared memory per home particle
 constexpr int kScanTile = 4096;      // cells per block of the cell-count scan (4 per thread)
 
 enum StepMode

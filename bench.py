@@ -271,13 +271,13 @@ def run_native(args) -> dict:
     ext = torch.zeros((system.n, 3), dtype=torch.float32).pin_memory().numpy()
     e2e_steps = max(steps, 20)
     for _ in range(3):
-        net.setExternalForces(ext)
+        net.setExternalForces(ext, wait=False)
         net.computeStep(1)
         net.energies()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        net.setExternalForces(ext)
+        net.setExternalForces(ext, wait=False)
         net.computeStep(1)
         net.energies()
     t1 = time.perf_counter()
@@ -305,9 +305,10 @@ def run_native(args) -> dict:
         "gpu_launches": int(launches),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(system.n * 12 + 4),
                 "d2h_bytes_per_step": CTL_BYTES,
-                "path": "bs_set_external_forces (pinned float[3n], copied straight to the device) + "
-                        "bs_step(1) + bs_get_energies per step; the energies come with the control "
-                        "block bs_step reads back to check the step"},
+                "path": "bs_set_external_forces_async (pinned float[3n], copied straight to the device "
+                        "in stream order) + bs_step(1) + bs_get_energies per step: one wait per step, "
+                        "in bs_step; the energies come with the control block bs_step reads back to "
+                        "check the step"},
         "roofline": {
             "bound": "hbm",
             "kernel": "k_step (forces + Euler step)",
@@ -485,12 +486,12 @@ def run_interactive(system=None, every: int = 10, frames: int = 50) -> dict:
     ext = torch.zeros((s.n, 3), dtype=torch.float32).pin_memory().numpy()
     ext[:100, 0] = 1e-3
     for _ in range(3):
-        net.setExternalForces(ext)
+        net.setExternalForces(ext, wait=False)
         net.computeStep(every)
         net.getPositions()
     t0 = time.perf_counter()
     for _ in range(frames):
-        net.setExternalForces(ext)
+        net.setExternalForces(ext, wait=False)
         net.computeStep(every)
         xyz = net.getPositions()
     dt = (time.perf_counter() - t0) / frames
@@ -499,7 +500,7 @@ def run_interactive(system=None, every: int = 10, frames: int = 50) -> dict:
     return {"frame_rate_hz": 1.0 / dt, "ms_per_frame": dt * 1e3, "steps_per_frame": every,
             "value": s.n * every / dt, "unit": UNIT,
             "h2d_bytes_per_frame": int(s.n * 12 + 4), "d2h_bytes_per_frame": int(s.n * 12 + CTL_BYTES),
-            "how": "bs_set_external_forces + bs_step(every) + bs_get_positions per frame, wall clock"}
+            "how": "bs_set_external_forces_async + bs_step(every) + bs_get_positions per frame, wall clock"}
 
 
 def run_adjoint(reps: int = 5) -> dict:

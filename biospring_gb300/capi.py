@@ -141,6 +141,7 @@ SIGNATURES = {
     "bs_set_velocities": (C.c_int, [C.c_void_p, _f32p]),
     "bs_set_force": (C.c_int, [C.c_void_p, C.c_int64, _f32p]),
     "bs_set_external_forces": (C.c_int, [C.c_void_p, _f32p]),
+    "bs_set_external_forces_async": (C.c_int, [C.c_void_p, _f32p]),
     "bs_get_energies": (C.c_int, [C.c_void_p, _f64p]),
     "bs_get_pairs": (C.c_int, [C.c_void_p, C.c_int32, _i64p, C.c_int64, _i64p]),
     "bs_get_cells": (C.c_int, [C.c_void_p, C.c_int32, _i64p]),

@@ -1678,7 +1678,19 @@ int bs_launch_phase(bs_sim *s, int32_t phase)
     return BS_OK;
 }
 
+static int set_external_forces(bs_sim *s, const float *f, bool wait);
+
 int bs_set_external_forces(bs_sim *s, const float *f)
+{
+    return set_external_forces(s, f, true);
+}
+
+int bs_set_external_forces_async(bs_sim *s, const float *f)
+{
+    return set_external_forces(s, f, false);
+}
+
+static int set_external_forces(bs_sim *s, const float *f, bool wait)
 {
     if (!s)
         return fail(nullptr, BS_E_ARG, "null handle");
@@ -1688,9 +1700,9 @@ int bs_set_external_forces(bs_sim *s, const float *f)
         return fail(s, BS_E_STATE, "external forces are not available for batched ensembles");
     if (!f)
         return fail(s, BS_E_ARG, "bs_set_external_forces: null forces");
-    // Copied at once, in stream order after the enqueued steps: straight from the caller's buffer
-    // when it is page-locked, else through the handle's pinned staging buffer. The call returns
-    // when the copy is done, so the caller may reuse f.
+    // Copied in stream order after the enqueued steps: straight from the caller's buffer when it
+    // is page-locked, else through the handle's pinned staging buffer. With wait (or a pageable
+    // buffer) the call returns when the copy is done, so the caller may reuse f.
     const size_t bytes = sizeof(float) * 3 * static_cast<size_t>(s->n);
     cudaPointerAttributes attr{};
     const bool pinned = cudaPointerGetAttributes(&attr, f) == cudaSuccess && attr.type == cudaMemoryTypeHost;
@@ -1702,7 +1714,8 @@ int bs_set_external_forces(bs_sim *s, const float *f)
     }
     BS_CUDA(cudaMemcpyAsync(s->p.ext, pinned ? f : s->ext_stage, bytes, cudaMemcpyHostToDevice, s->stream));
     BS_CUDA(cudaMemcpyAsync(&s->p.ctl->ext_pending, s->one_host, sizeof(int), cudaMemcpyHostToDevice, s->stream));
-    BS_CUDA(cudaStreamSynchronize(s->stream));
+    if (wait || !pinned)
+        BS_CUDA(cudaStreamSynchronize(s->stream));
     return BS_OK;
 }
 

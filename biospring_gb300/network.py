@@ -274,9 +274,13 @@ class SpringNetwork:
         f = _f32(f)
         self._check(self._lib.bs_set_force(self._h, int(i), ptr(f, C.c_float)), self._h)
 
-    def setExternalForces(self, f):
+    def setExternalForces(self, f, wait: bool = True):
+        """Every particle's external force for the next step. wait=False enqueues the upload
+        without waiting: f must then be page-locked and stay unchanged until the next
+        synchronising call (computeStep, a getter)."""
         f = _f32(f, (-1, 3))
-        self._check(self._lib.bs_set_external_forces(self._h, ptr(f, C.c_float)), self._h)
+        fn = self._lib.bs_set_external_forces if wait else self._lib.bs_set_external_forces_async
+        self._check(fn(self._h, ptr(f, C.c_float)), self._h)
 
     def energies(self) -> dict:
         out = np.zeros(6, dtype=np.float64)

@@ -296,8 +296,15 @@ int bs_set_velocities(bs_sim *sim, const float *vel);
 int bs_set_force(bs_sim *sim, int64_t i, const float f[3]);
 
 /* Sets the external force of every particle for the next step (float[3n], caller order);
- * the bulk form of bs_set_force used by interactive drivers every step. */
+ * the bulk form of bs_set_force used by interactive drivers every step. Returns when the copy is
+ * done: the caller may reuse f at once. */
 int bs_set_external_forces(bs_sim *sim, const float *f);
+
+/* The same, enqueued on the handle's stream without waiting: f must be page-locked and must stay
+ * unchanged until the next call that waits for the stream (bs_step, bs_synchronize, a getter);
+ * an interactive driver alternates two buffers. A pageable f is copied as bs_set_external_forces
+ * does. Saves the wait of a step's force upload. */
+int bs_set_external_forces_async(bs_sim *sim, const float *f);
 
 /* Probe position and velocity (float[6]: x, y, z, vx, vy, vz) after the last step; zeros when
  * probe.enable is off (replaces SpringNetwork::getProbeParticle, SpringNetwork.h:277). The probe

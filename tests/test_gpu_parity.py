@@ -315,6 +315,30 @@ def test_external_force_applies_for_one_step():
     assert dv < 0.5 * dt
 
 
+@pytest.mark.parametrize("wait", [True, False], ids=["sync", "async"])
+def test_bulk_external_forces_apply_for_one_step(wait):
+    """bs_set_external_forces and its enqueued form: the forces act on the next step only, like
+    SpringNetwork::setForce, and the enqueued upload from a page-locked buffer gives the same
+    trajectory as the waiting one."""
+    import torch
+    from biospring_gb300 import workloads as W
+    s = W.ca_network(n=300, seed=3)
+    a = gpu_network(s)
+    b = gpu_network(s)
+    f = torch.zeros((s.n, 3), dtype=torch.float32).pin_memory().numpy()
+    f[5, 0] = 0.5
+    f[17] = [0.0, -0.25, 0.125]
+    a.setForce(5, [0.5, 0.0, 0.0])
+    a.setForce(17, [0.0, -0.25, 0.125])
+    b.setExternalForces(f, wait=wait)
+    a.computeStep(1)
+    b.computeStep(1)
+    np.testing.assert_array_equal(a.getVelocities(), b.getVelocities())
+    a.computeStep(2)
+    b.computeStep(2)
+    np.testing.assert_array_equal(a.getPositions(), b.getPositions())
+
+
 def test_errors_match_reference_exceptions():
     from biospring_gb300 import BsError, SpringNetwork, capi
     net = SpringNetwork()

@@ -246,11 +246,13 @@ def run_native(args) -> dict:
     if dist is not None:
         dist.barrier()
     clocks = sampler.stop()
-    net.synchronize()
+    # steps the timed launches completed, read before synchronize() would complete any that a
+    # drift past half the list skin stopped (those would make the timed figure too fast)
     done = net.stepCount() - step0
+    net.synchronize()
     launches = net.launchCount() - launches0
     if done != steps:
-        raise RuntimeError(f"timed region completed {done} of {steps} steps (a stale list forced a redo)")
+        raise RuntimeError(f"timed region completed {done} of {steps} steps (a stale list stopped the rest)")
     step_ms = [ev[i][0].elapsed_time(ev[i][2]) for i in range(steps)]
     kern_ms = [ev[i][1].elapsed_time(ev[i][2]) for i in range(steps)]
     total_ms = max_over_ranks(float(sum(step_ms)), dist, "cuda")

@@ -48,8 +48,9 @@ UNIT = "particle-steps/s"
 N_PARTICLES = 100_000
 BOX = 160.0
 REBUILD = 10
-# Verlet buffer of the device pair list: a particle drifts about 2e-4 A per 10-step period here,
-# so a 0.1 A skin keeps a margin of two orders of magnitude before a drift check forces a rebuild
+# Verlet buffer of the device pair list. The largest drift of a particle over a 10-step period
+# here grows from 4e-5 A at the start to 3e-3 A after 1,000 steps and 1.1e-2 A after 5,000, so a
+# 0.1 A skin (a rebuild is forced past half of it) keeps a margin of 4.6 or more over 5,000 steps
 LIST_SKIN = 0.1
 STEP_BYTES_PER_PARTICLE_BASE = 84.0   # positions r+w 32, velocities r+w 32, parameters 16, row pointer 4
 SPRING_BYTES_PER_ENTRY = 12.0         # partner index + stiffness + rest length

@@ -34,6 +34,10 @@ namespace
 
 namespace cg = cooperative_groups;
 
+// the batched list build loads a warp's next home while it lists the current one
+#ifndef BS_BPL_PREFETCH
+#define BS_BPL_PREFETCH 1
+#endif
 constexpr int kBatchBboxBlock = 256;
 constexpr int kBatchPlWarps = 8;
 constexpr int kMaxSysCells = 1 << 26; // a system spread wider than this falls back to one cell
@@ -222,9 +226,36 @@ __global__ void __launch_bounds__(kBatchPlWarps * 32) k_batch_pairlist(Params p)
     const int cap0 = p.pl[0].cap, cap1 = p.pl[1].cap, cap2 = p.pl[2].cap, cap3 = p.pl[3].cap;
     const size_t stride = static_cast<size_t>(p.npad);
     const unsigned int below = (1u << lane) - 1u;
-    for (int i = blockIdx.x * kBatchPlWarps + wid; i < p.n; i += gridDim.x * kBatchPlWarps)
+    // Each warp lists homes i, i + istride, ...; the next home's own data (flags, position, cell,
+    // system, spring degree) are loaded while the warp lists the current one, so a home's set-up
+    // starts one dependent round trip later in its chain.
+    const int istride = static_cast<int>(gridDim.x) * kBatchPlWarps;
+    int i = static_cast<int>(blockIdx.x) * kBatchPlWarps + wid;
+    unsigned int fi_n = 0u;
+    float4 pi_n = make_float4(0.f, 0.f, 0.f, 0.f);
+    int cell_n = 0, sys_n = 0, deg_n = 0;
+    auto fetch = [&](int h) {
+        if (h < p.n)
+        {
+            fi_n = fl[h];
+            pi_n = pos[h];
+            cell_n = p.cell_of[h];
+            if (BATCH)
+                sys_n = p.sys_of[h];
+            deg_n = p.spring_on ? p.se_deg[h] : 0;
+        }
+    };
+    if (BS_BPL_PREFETCH)
+        fetch(i);
+    for (; i < p.n; i += istride)
     {
-        const unsigned int fi = fl[i];
+        if (!BS_BPL_PREFETCH)
+            fetch(i);
+        const unsigned int fi = fi_n;
+        const float4 pi = pi_n;
+        const int cell_i = cell_n, sys_i = sys_n, deg = deg_n;
+        if (BS_BPL_PREFETCH)
+            fetch(i + istride);
         const bool dyn = !(fi & PF_STATIC);
         const bool on0 = dyn && l0;
         const bool on1 = dyn && l1 && ((fi & PF_CHARGED) || p.coul_all);
@@ -239,21 +270,19 @@ __global__ void __launch_bounds__(kBatchPlWarps * 32) k_batch_pairlist(Params p)
         bool wide = false;
         if (on0 || on1 || on2)
         {
-            const float4 pi = pos[i];
             int cbase = 0, nx = ctl->gnx, ny = ctl->gny, nz = ctl->gnz;
             if (BATCH)
             {
-                const int b = p.sys_of[i];
+                const int b = sys_i;
                 cbase = p.sys_cells[b];
                 nx = p.sys_grid[b].nx;
                 ny = p.sys_grid[b].ny;
                 nz = p.sys_grid[b].nz;
             }
-            const int lc = p.cell_of[i] - cbase;
+            const int lc = cell_i - cbase;
             const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
             // spring partners of i in registers: lane m holds partners m and m + 32 (slots, -1 for
             // none); a home with more than 64 compares every candidate with its ELL row
-            const int deg = p.spring_on ? p.se_deg[i] : 0;
             const bool small = deg <= 64;
             const int ps0 = small && lane < deg ? static_cast<int>(p.se_col[static_cast<size_t>(lane) * stride + i] & kSlotMask) : -1;
             const int ps1 =

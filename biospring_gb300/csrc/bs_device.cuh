@@ -978,10 +978,12 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
     constexpr bool kHoist = BS_HOIST && LEAN && SINGLE;
     int cnt0 = -1;
     uint2 w0 = make_uint2(0u, 0u);
+    float fhi_i = 0.0f;
     if (s < send)
     {
         pi = pos[s];
         fi = p.flags[lb][s];
+        fhi_i = p.fhi[lb][s];
         if (kHoist && p.steric_on && p.lj_uniform && p.pl16)
         {
             const PairList &L = p.pl[0];
@@ -997,7 +999,6 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
         if (p.steric_on)
         {
             float sx = 0.f, sy = 0.f, sz = 0.f, es = 0.f;
-            const float fhi_i = p.fhi[lb][s];
             if (LEAN && p.lj_uniform && p.pl16)
                 steric_forces_batched<SM, T, true, true>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es, cnt0, w0);
             else if ((SINGLE && BS_GATHER) || (!SINGLE && BS_GATHER_BATCH))
@@ -1011,7 +1012,8 @@ __device__ __forceinline__ int particle_step(const Params &p, const int s, const
                 steric_forces<SM, T, 0>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
             else
                 steric_forces<SM, T, 1>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
-            if (p.pl[kListStericStatic].cnt[s] > 0)
+            // the static-partner list exists only when some particle is static
+            if (p.pl[kListStericStatic].on && p.pl[kListStericStatic].cnt[s] > 0)
                 steric_forces<SM, T, 2>(p, s, t, pi, fhi_i, pos, p.fhi[lb], sx, sy, sz, es);
             const float kf = p.k_spring_f * p.steric_scale;
             fx = fmaf(sx, kf, fx);

@@ -59,7 +59,7 @@ CTL_BYTES = 288                       # device control block (status, step count
 # DRAM bytes (read + write) of one k_step launch on this workload after an L2 flush, from one ncu
 # capture of dram__bytes_read.sum + dram__bytes_write.sum, and the digest of the step kernel's
 # sources that capture ran on: when the sources have changed since, the line marks the figure stale.
-STEP_KERNEL_TRAFFIC = {"bytes": 69.888512e6 + 1.794048e6, "sources_sha": "07ab4b2f679d5cfd", "captured": "2026-12-04"}
+STEP_KERNEL_TRAFFIC = {"bytes": 69.48992e6 + 1.682176e6, "sources_sha": "d0671f577e273adc", "captured": "2026-12-04"}
 STEP_KERNEL_SOURCES = ("biospring_gb300/csrc/bs_device.cuh", "biospring_gb300/csrc/bs_kernels.cu",
                        "biospring_gb300/csrc/bs_kernels.cuh", "biospring_gb300/csrc/bs_common.cuh")
 DIELECTRIC_NOTE = ("Coulomb eps = 4r (distance-dependent), as the 100k configuration states; the reference's "
